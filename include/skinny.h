@@ -1,0 +1,146 @@
+/* skinny.h -- C ABI of the GB300 (sm_103a) tall-skinny product library.
+ *
+ * Drop-in boundary for te42kyfo/skinny_matmul's templated launchers, whose common shape is
+ * MatmulFunctionType (versions.hpp:43-45):
+ *   bool f(size_t blockCount, int M, int N, int K, const T* A, int lda, T alpha,
+ *          const T* B, int ldb, T beta, T* C, int ldc)
+ *
+ * Layouts (unchanged from the reference; all pointers are DEVICE pointers owned by the caller):
+ *   TSMTTSM  C[n*ldc+m] = alpha * sum_k A[k*lda+m] * B[k*ldb+n] + beta * C[n*ldc+m]
+ *            A: K x M row-major, B: K x N row-major, C: M x N with column stride ldc.
+ *            A == B with lda == ldb and M == N is the Gram (SELF) mode.
+ *   TSMM     C[r*ldc+n] = alpha * sum_m A[r*lda+m] * B[n*ldb+m] + beta * C[r*ldc+n]
+ *            A: K x M row-major, B: M x N stored column by column (B[n*ldb+m]), C: K x N.
+ *            A == C (with lda == ldc) is the in-place form; each output row is computed from
+ *            that row's old contents.
+ *   Complex values are interleaved (re, im) as cuFloatComplex / cuDoubleComplex; products use
+ *   the plain transpose, not the conjugate (the reference's cuBLAS oracle uses OP_T,
+ *   tsmttsm/gen_cublas.cuh:29-39).
+ *   beta == 0 means C is not read (tsmm/fix3.cuh:31-35 BETAISZERO; BLAS convention).
+ *
+ * Differences from the reference, all deliberate:
+ *   - every call returns a status and never exits the process (the reference aborts through
+ *     GPU_ERROR, gpu_error.cuh:4-13);
+ *   - sizes and leading dimensions are 64-bit in the skinny_* entry points;
+ *   - M and N are runtime values (the reference compiles one binary per (M, N), Makefile:11-20);
+ *   - calls are stream-ordered on the stream given; the reference-shaped entry points use the
+ *     legacy default stream, as the reference does;
+ *   - workspace is owned by a handle, one buffer per stream, so concurrent streams never share a
+ *     partial-sum buffer (the reference keeps one static buffer per kernel family,
+ *     tsmttsm/genv5.cuh:91).
+ */
+#ifndef SKINNY_H
+#define SKINNY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SKINNY_OK = 0,
+  SKINNY_UNSUPPORTED = 1, /* shape / dtype / method combination not provided (reference: return false) */
+  SKINNY_BAD_ARG = 2,     /* invalid sizes, leading dimensions, null pointers or aliasing */
+  SKINNY_NO_MEM = 3,      /* workspace allocation failed or request over the memory budget */
+  SKINNY_TIMEOUT = 4,     /* a bounded device-side wait gave up; the device stays usable */
+  SKINNY_DEVICE_ERROR = 5,/* CUDA reported an error */
+  SKINNY_NOT_READY = 6    /* request-loop ticket not finished yet */
+} skinny_status;
+
+typedef enum {
+  SKINNY_R32 = 0, /* float                       */
+  SKINNY_R64 = 1, /* double                      */
+  SKINNY_C32 = 2, /* cuFloatComplex  (float re, im)  */
+  SKINNY_C64 = 3  /* cuDoubleComplex (double re, im) */
+} skinny_dtype;
+
+typedef enum {
+  SKINNY_ACC_NATIVE = 0, /* accumulate in the working type (reference dItype == dtype) */
+  SKINNY_ACC_DD = 1,     /* double-double accumulation, R64 only (reference dItype == PseudoQuad, types.hpp:49-57) */
+  SKINNY_ACC_SPLIT = 2,  /* R64 split precision: FP64 sliced into BF16 digits, products on tcgen05
+                            tensor cores with exact FP32 accumulation, recombined in FP64.  No
+                            counterpart in the reference. */
+  SKINNY_ACC_AUTO = 3    /* fastest method meeting the working precision's error bound */
+} skinny_acc;
+
+typedef struct { float x, y; } skinny_c32;  /* same layout as cuFloatComplex  */
+typedef struct { double x, y; } skinny_c64; /* same layout as cuDoubleComplex */
+
+typedef struct skinny_handle_st* skinny_handle;
+
+/* Handle: device, per-stream workspaces, autotune table.  One handle may be used from several
+ * host threads; calls on the same stream are serialised in stream order. */
+skinny_status skinny_create(skinny_handle* handle, int device);
+skinny_status skinny_destroy(skinny_handle handle);
+const char* skinny_status_string(skinny_status s);
+/* Detail message of the last failing call on this host thread ("" if none). */
+const char* skinny_last_error(void);
+/* Synchronises the device and reports SKINNY_TIMEOUT if a kernel's bounded wait gave up since
+ * the last check (the flag is then cleared and the handle's workspaces are reset). */
+skinny_status skinny_check_device(skinny_handle handle);
+
+/* TSMTTSM, replaces tsmttsm/genv{3,3x,5,6,7,8}.cuh, specsmall.cuh (+ their deviceReduce) and
+ * tsmttsm/gen_cublas.cuh:12-46.  alpha/beta point to one HOST value of the dtype. */
+skinny_status skinny_tsmttsm(skinny_handle handle, skinny_dtype dtype, skinny_acc acc, int64_t M,
+                             int64_t N, int64_t K, const void* A, int64_t lda, const void* alpha,
+                             const void* B, int64_t ldb, const void* beta, void* C, int64_t ldc,
+                             void* stream);
+
+/* TSMM, replaces tsmm/fix{1,2,3,4}.cuh, fix_fb.cuh, var1.cuh, varip{1,2,3}.cuh,
+ * fix_ip_ghost.cuh, var_ip_ghost.cuh, the blends (fix_blend.cuh:7-29, varip_blend.cuh:8-29) and
+ * tsmm/cublas.cuh:18-62. */
+skinny_status skinny_tsmm(skinny_handle handle, skinny_dtype dtype, skinny_acc acc, int64_t M,
+                          int64_t N, int64_t K, const void* A, int64_t lda, const void* alpha,
+                          const void* B, int64_t ldb, const void* beta, void* C, int64_t ldc,
+                          void* stream);
+
+/* SVQB orthogonalisation of X (K x M row-major, ldx >= M, FP64), in place, entirely on the
+ * device; replaces svqb/svqb.cu:72-130 (which runs the eigensolve on the host through MAGMA).
+ *   S = X^T X (gram_acc selects the method), d_i = 1/sqrt(S_ii) (0 if S_ii <= 1e-15),
+ *   S <- D S D, S = U L U^T (Jacobi, FP64), T = D U diag(1/sqrt(max(1e-15, l))),
+ *   X <- X T (in-place TSMM).
+ * If orth_err_out is non-null, ||Q^T Q - I||_F is computed on the device (double-double Gram)
+ * and written there after a stream synchronisation (svqb/svqb.cu:184-211 getL2Error). */
+skinny_status skinny_svqb(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M,
+                          double* X, int64_t ldx, double* orth_err_out, void* stream);
+
+/* ---- Reference-shaped entry points ---------------------------------------------------------
+ * Exactly MatmulFunctionType (versions.hpp:43-45).  They run on the legacy default stream with a
+ * per-device default handle, like the reference's launchers (e.g. tsmttsm/genv5.cuh:93-114,
+ * tsmm/fix3.cuh:41-65).  Return 1 when the product was launched, 0 when it was not (unsupported
+ * shape, or an error: see skinny_last_error()).  blockCount is accepted for signature
+ * compatibility and ignored: the grid is sized from the SM count.
+ * The _dd variants take double data and accumulate in double-double (the reference's
+ * dItype == PseudoQuad). */
+int skinny_tsmttsm_s(size_t blockCount, int M, int N, int K, const float* A, int lda, float alpha,
+                     const float* B, int ldb, float beta, float* C, int ldc);
+int skinny_tsmttsm_d(size_t blockCount, int M, int N, int K, const double* A, int lda, double alpha,
+                     const double* B, int ldb, double beta, double* C, int ldc);
+int skinny_tsmttsm_c(size_t blockCount, int M, int N, int K, const skinny_c32* A, int lda,
+                     skinny_c32 alpha, const skinny_c32* B, int ldb, skinny_c32 beta, skinny_c32* C,
+                     int ldc);
+int skinny_tsmttsm_z(size_t blockCount, int M, int N, int K, const skinny_c64* A, int lda,
+                     skinny_c64 alpha, const skinny_c64* B, int ldb, skinny_c64 beta, skinny_c64* C,
+                     int ldc);
+int skinny_tsmttsm_dd(size_t blockCount, int M, int N, int K, const double* A, int lda, double alpha,
+                      const double* B, int ldb, double beta, double* C, int ldc);
+
+int skinny_tsmm_s(size_t blockCount, int M, int N, int K, const float* A, int lda, float alpha,
+                  const float* B, int ldb, float beta, float* C, int ldc);
+int skinny_tsmm_d(size_t blockCount, int M, int N, int K, const double* A, int lda, double alpha,
+                  const double* B, int ldb, double beta, double* C, int ldc);
+int skinny_tsmm_c(size_t blockCount, int M, int N, int K, const skinny_c32* A, int lda,
+                  skinny_c32 alpha, const skinny_c32* B, int ldb, skinny_c32 beta, skinny_c32* C,
+                  int ldc);
+int skinny_tsmm_z(size_t blockCount, int M, int N, int K, const skinny_c64* A, int lda,
+                  skinny_c64 alpha, const skinny_c64* B, int ldb, skinny_c64 beta, skinny_c64* C,
+                  int ldc);
+int skinny_tsmm_dd(size_t blockCount, int M, int N, int K, const double* A, int lda, double alpha,
+                   const double* B, int ldb, double beta, double* C, int ldc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKINNY_H */

@@ -1,0 +1,147 @@
+"""Host-side mirror of the reference's launcher interface, over the C ABI.
+
+The reference exposes one launcher per kernel variant with the shape (versions.hpp:43-45)
+    bool f(blockCount, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc)
+and its harness keeps them in a list of (function, name) pairs (versions.hpp:48-177,
+test.cu:251-301).  `launchers(op, dtype)` returns the same kind of list for this library, and
+`tsmttsm` / `tsmm` / `svqb` are the stream-aware calls of include/skinny.h.  Device buffers are
+torch CUDA tensors (flat storage in the reference layout) or raw device addresses (int).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Callable, List, Tuple
+
+from . import lib as L
+
+_ACC = {"native": L.ACC_NATIVE, "dd": L.ACC_DD, "split": L.ACC_SPLIT, "auto": L.ACC_AUTO}
+
+
+def _dtype_code(t) -> int:
+    import torch
+    m = {torch.float32: L.R32, torch.float64: L.R64, torch.complex64: L.C32, torch.complex128: L.C64}
+    if t.dtype not in m:
+        raise TypeError(f"unsupported dtype {t.dtype}")
+    return m[t.dtype]
+
+
+def _scalar(v, code):
+    if code == L.R32:
+        return ctypes.c_float(float(v))
+    if code == L.R64:
+        return ctypes.c_double(float(v))
+    v = complex(v)
+    return (L.c32 if code == L.C32 else L.c64)(v.real, v.imag)
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Handle:
+    """Owns a skinny_handle (device, per-stream workspaces, autotune table)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.skinny_create(ctypes.byref(h), device))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            self.lib.skinny_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check_device(self):
+        return L.check(self.lib.skinny_check_device(self.h))
+
+    def _product(self, fn, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc, stream, dtype):
+        code = dtype if dtype is not None else _dtype_code(A if not isinstance(A, int) else C)
+        al, be = _scalar(alpha, code), _scalar(beta, code)
+        st = fn(self.h, code, _ACC[acc], M, N, K, _ptr(A), lda, ctypes.byref(al), _ptr(B), ldb,
+                ctypes.byref(be), _ptr(C), ldc, _stream(stream))
+        return L.check(st)
+
+    def tsmttsm(self, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, dtype=None):
+        """C[n*ldc+m] = alpha * sum_k A[k*lda+m] B[k*ldb+n] + beta * C[n*ldc+m]."""
+        return self._product(self.lib.skinny_tsmttsm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc,
+                             acc, stream, dtype)
+
+    def tsmm(self, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, dtype=None):
+        """C[r*ldc+n] = alpha * sum_m A[r*lda+m] B[n*ldb+m] + beta * C[r*ldc+n]  (A may be C)."""
+        return self._product(self.lib.skinny_tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc,
+                             acc, stream, dtype)
+
+    def svqb(self, K, M, X, ldx, gram_acc="split", orth_err=True, stream=None):
+        """In-place SVQB of X (K x M, FP64); returns ||Q^T Q - I||_F when orth_err."""
+        err = ctypes.c_double(-1.0)
+        L.check(self.lib.skinny_svqb(self.h, _ACC[gram_acc], K, M, _ptr(X), ldx,
+                                     ctypes.byref(err) if orth_err else None, _stream(stream)))
+        return err.value if orth_err else None
+
+
+_default: dict = {}
+
+
+def default_handle(device: int | None = None) -> Handle:
+    if device is None:
+        import torch
+        device = torch.cuda.current_device()
+    if device not in _default:
+        _default[device] = Handle(device)
+    return _default[device]
+
+
+def tsmttsm(M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, handle=None):
+    return (handle or default_handle()).tsmttsm(M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc, stream)
+
+
+def tsmm(M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, handle=None):
+    return (handle or default_handle()).tsmm(M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc, stream)
+
+
+def svqb(K, M, X, ldx, gram_acc="split", orth_err=True, stream=None, handle=None):
+    return (handle or default_handle()).svqb(K, M, X, ldx, gram_acc, orth_err, stream)
+
+
+_REF_SUFFIX = {"float32": "s", "float64": "d", "complex64": "c", "complex128": "z", "dd": "dd"}
+
+
+def launchers(op: str, dtype: str) -> List[Tuple[Callable, str]]:
+    """Reference-shaped launchers for `op` ("tsmttsm" | "tsmm") and `dtype`, as (fn, name) pairs
+    like getEnabledTSMTTSMVersions / getEnabledTSMMVersions (versions.hpp:48-177).
+    fn(blockCount, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc) -> bool, on the legacy default
+    stream.  A, B, C are device addresses (int) or tensors."""
+    lib = L.load()
+    sfx = _REF_SUFFIX[dtype]
+    raw = getattr(lib, f"skinny_{op}_{sfx}")
+    cplx = sfx in ("c", "z")
+    ct = {"s": ctypes.c_float, "d": ctypes.c_double, "dd": ctypes.c_double, "c": L.c32, "z": L.c64}[sfx]
+
+    def fn(blockCount, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc):
+        conv = (lambda v: ct(complex(v).real, complex(v).imag)) if cplx else (lambda v: ct(v))
+        P = ctypes.POINTER(ct)
+        return bool(raw(blockCount, M, N, K, ctypes.cast(_ptr(A), P), lda, conv(alpha),
+                        ctypes.cast(_ptr(B), P), ldb, conv(beta), ctypes.cast(_ptr(C), P), ldc))
+
+    return [(fn, f"GB300_{op.upper()}_{sfx.upper()}")]

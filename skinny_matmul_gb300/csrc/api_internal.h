@@ -1,0 +1,68 @@
+// api_internal.h -- handle layout and internal entry points shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "launch.cuh"
+#include "skinny.h"
+
+struct skinny_handle_st {
+  explicit skinny_handle_st(int device);
+  skinny::DeviceInfo dev;
+  std::mutex mu;                                        // guards ws / tune / extra state
+  std::map<cudaStream_t, skinny::Workspace> ws;         // one partial-sum buffer per stream
+  std::map<std::tuple<int, int, int, int64_t, int64_t>, skinny::LaunchOpts> tune;  // autotuner table
+  std::vector<void*> extra_allocs;                       // buffers owned by other subsystems
+  std::map<cudaStream_t, void*> split_ws;                // split-precision scratch per stream
+  std::map<cudaStream_t, size_t> split_ws_bytes;
+  std::map<cudaStream_t, void*> svqb_ws;                 // SVQB scratch per stream
+  int* err = nullptr;                                    // device error word (bounded waits)
+
+  // launch options recorded by the autotuner for (op, dtype, acc, M, N); defaults otherwise
+  skinny::LaunchOpts tuned(bool tsmm, skinny_dtype dt, skinny_acc acc, int64_t M, int64_t N) {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = tune.find(std::make_tuple((int)tsmm, (int)dt, (int)acc, M, N));
+    return it == tune.end() ? skinny::LaunchOpts{} : it->second;
+  }
+};
+
+namespace skinny {
+
+struct DevGuard {
+  explicit DevGuard(int d);
+  ~DevGuard();
+  int prev = 0;
+  bool changed = false;
+};
+
+size_t dtype_size(skinny_dtype dt);
+skinny_handle default_handle();
+
+skinny_status check_args(bool tsmm, skinny_dtype dt, int64_t M, int64_t N, int64_t K,
+                         const void* A, int64_t lda, const void* alpha, const void* B,
+                         int64_t ldb, const void* beta, const void* C, int64_t ldc);
+
+// Full product entry (argument checks, device guard, handle lock, dispatch).
+skinny_status product(skinny_handle h, bool tsmm, skinny_dtype dt, skinny_acc acc, int64_t M,
+                      int64_t N, int64_t K, const void* A, int64_t lda, const void* alpha,
+                      const void* B, int64_t ldb, const void* beta, void* C, int64_t ldc,
+                      void* stream, const LaunchOpts* opts);
+
+// Dispatch without checks or locking (caller holds h->mu and the device guard).
+skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skinny_acc acc,
+                               int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
+                               const void* alpha, const void* B, int64_t ldb, const void* beta,
+                               void* C, int64_t ldc, cudaStream_t st, const LaunchOpts& o);
+
+// FP64 split-precision (tensor-core) products; SKINNY_UNSUPPORTED when the shape is not covered
+// (for auto == true the caller then falls back to the CUDA-core FP64 kernels).
+skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, int64_t K,
+                            const double* A, int64_t lda, const void* alpha, const double* B,
+                            int64_t ldb, const void* beta, double* C, int64_t ldc,
+                            cudaStream_t st, bool autoselect);
+
+}  // namespace skinny

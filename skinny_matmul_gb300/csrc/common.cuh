@@ -1,0 +1,174 @@
+// common.cuh -- arithmetic types, accumulation rules and PTX helpers shared by every kernel.
+//
+// Accumulation rules restate the reference's type-generic helpers:
+//   real      acc += a*b                      (cu_complex.h:84-89 axpy)
+//   complex   acc += a*b, plain product       (cu_complex.h:127-131, no conjugate)
+//   dd        PseudoQuad axpy2 / accu / scale2 / renormalize / convert
+//             (PseudoQuad.cuh:96-108, 66-75, 80-86, 137-140, 149-152)
+// Epilogue:   C = beta*C + alpha*S, and C = alpha*S (C not read) when beta == 0
+//             (genv5.cuh:25, specsmall.cuh:139-140, tsmm/fix3.cuh:31-35).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace skinny {
+
+struct dd {
+  double s, t;
+};
+template <typename R>
+struct __align__(2 * sizeof(R)) cplx {
+  R x, y;
+};
+typedef cplx<float> c32;
+typedef cplx<double> c64;
+
+// ---------------------------------------------------------------- double-double primitives
+__device__ __forceinline__ dd dd_fast2sum(double a, double b) {
+  double s = __dadd_rn(a, b);
+  double z = __dadd_rn(s, -a);
+  return {s, __dadd_rn(b, -z)};
+}
+__device__ __forceinline__ dd dd_gen2sum(double a, double b) {
+  double s = __dadd_rn(a, b);
+  double ap = __dadd_rn(s, -b);
+  double bp = __dadd_rn(s, -ap);
+  double da = __dadd_rn(a, -ap);
+  double db = __dadd_rn(b, -bp);
+  return {s, __dadd_rn(da, db)};
+}
+__device__ __forceinline__ dd dd_accu(dd x, dd y) {
+  dd s = dd_gen2sum(x.s, y.s);
+  dd t = dd_gen2sum(x.t, y.t);
+  double c = __dadd_rn(s.t, t.s);
+  dd v = dd_fast2sum(s.s, c);
+  double w = __dadd_rn(t.t, v.t);
+  return dd_fast2sum(v.s, w);
+}
+__device__ __forceinline__ dd dd_axpy2(dd c, double a, double b) {
+  dd r;
+  r.s = __fma_rn(a, b, c.s);
+  double abp = __dadd_rn(r.s, -c.s);
+  double cp = __dadd_rn(r.s, -abp);
+  double dab = __fma_rn(a, b, -abp);
+  double dc = __dadd_rn(c.s, -cp);
+  r.t = __dadd_rn(__dadd_rn(dc, dab), c.t);
+  return r;
+}
+__device__ __forceinline__ dd dd_scale2(dd a, double b) {
+  double s = __dmul_rn(a.s, b);
+  double t = __fma_rn(a.s, b, -s);
+  t = __fma_rn(a.t, b, t);
+  return dd_fast2sum(s, t);
+}
+
+// ---------------------------------------------------------------- accumulation traits
+// Ops<T, Acc>: T is the storage/working type, Acc the accumulator.
+template <typename T, typename Acc>
+struct Ops;
+
+template <typename R>
+struct Ops<R, R> {  // float / double
+  static __device__ __forceinline__ R zero() { return R(0); }
+  static __device__ __forceinline__ R mac(R acc, R a, R b) { return fma(a, b, acc); }
+  static __device__ __forceinline__ R add(R x, R y) { return x + y; }
+  static __device__ __forceinline__ bool is_zero(R v) { return v == R(0); }
+  static __device__ __forceinline__ R finish(R s, R alpha, R beta, bool beta_zero, const R* c) {
+    return beta_zero ? alpha * s : (*c) * beta + s * alpha;
+  }
+  static __device__ __forceinline__ R shfl_xor(R v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+};
+
+template <typename R>
+struct Ops<cplx<R>, cplx<R>> {
+  typedef cplx<R> C;
+  static __device__ __forceinline__ C zero() { return {R(0), R(0)}; }
+  static __device__ __forceinline__ C mac(C acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+    return acc;
+  }
+  static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
+  static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+  static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
+    C r = mul(alpha, s);
+    if (!beta_zero) r = add(mul(beta, *c), r);
+    return r;
+  }
+  static __device__ __forceinline__ C shfl_xor(C v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
+  }
+};
+
+template <>
+struct Ops<double, dd> {  // double inputs, PseudoQuad accumulation
+  static __device__ __forceinline__ dd zero() { return {0.0, 0.0}; }
+  static __device__ __forceinline__ dd mac(dd acc, double a, double b) { return dd_axpy2(acc, a, b); }
+  static __device__ __forceinline__ dd add(dd x, dd y) { return dd_accu(x, y); }
+  static __device__ __forceinline__ double finish(dd s, double alpha, double beta, bool beta_zero,
+                                                  const double* c) {
+    double v = [&] {
+      dd r = dd_fast2sum(s.s, s.t);  // renormalize
+      r = dd_scale2(r, alpha);
+      return __dadd_rn(r.s, r.t);  // convert
+    }();
+    return beta_zero ? v : __dadd_rn(__dmul_rn(beta, *c), v);
+  }
+  static __device__ __forceinline__ dd shfl_xor(dd v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.t, o)};
+  }
+};
+
+// ---------------------------------------------------------------- device error word
+// Kernels never trap.  A wait that runs out of iterations records a code here and returns.
+enum : int { SKINNY_DEVERR_NONE = 0, SKINNY_DEVERR_TIMEOUT = 1 };
+
+// ---------------------------------------------------------------- PTX helpers (sm_90+ / sm_103a)
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// 1-D bulk copy global -> shared, completion counted on an mbarrier (TMA, no tensor map).
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: returns false (and records a timeout in *err) after max_iter polls.
+// try_wait itself suspends for a hardware-chosen interval, so 2^22 polls is well above a second.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+  for (uint32_t i = 0; i < (1u << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
+  return false;
+}
+
+__host__ __device__ constexpr int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace skinny

@@ -1,0 +1,84 @@
+// tsmm.cuh -- TSMM on CUDA cores: C(KxN) = alpha * A(KxM) B(MxN) + beta * C, C may be A.
+//
+// Replaces the reference's tsmm/fix{1,2,3,4}, fix_fb, var1, varip{1,2,3}, fix_ip_ghost and
+// var_ip_ghost kernels (tsmm/fix3.cuh:4-65, fix_fb.cuh:5-102, fix_ip_ghost.cuh:4-44 ...).
+// Same layouts: A[r*lda+m], B[n*ldb+m] (column n contiguous over m), C[r*ldc+n].
+//
+// Design:
+//   * B is staged once per CTA in shared memory as Bs[m][n] (n fastest), so a thread reads the
+//     TN consecutive columns it owns for each m without bank conflicts.
+//   * A thread owns one row and TN consecutive output columns (a "cell"); the gn cells of a row
+//     are consecutive lanes of one warp (gn is a power of two <= 32), so each row's outputs are
+//     written as one contiguous, coalesced run.
+//   * In place (A == C, lda == ldc): every lane finishes reading its row of A before the warp
+//     passes __syncwarp(), and only then are outputs written; rows never cross warps, so no
+//     output can overwrite input that another thread still needs.  beta*C reads the element the
+//     same thread then overwrites.
+//   * Rows are distributed grid-stride over a persistent grid; all lanes of a warp run the same
+//     trip count so the __syncwarp() is always reached by the full warp.
+#pragma once
+#include "common.cuh"
+#include "tsmttsm.cuh"  // tzero
+
+namespace skinny {
+
+template <typename T>
+struct TsmmArgs {
+  const T* A;
+  const T* B;
+  T* C;
+  int64_t K, lda, ldb, ldc;
+  int M, N;
+  T alpha, beta;
+  int beta_zero;
+  int gn;  // cells per row (power of two, <= 32)
+  int np;  // padded width of Bs (gn * TN)
+};
+
+constexpr int TSMM_THREADS = 256;
+
+template <typename T, typename Acc, int TN>
+__global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p) {
+  typedef Ops<T, Acc> O;
+  constexpr int NT = TSMM_THREADS;
+  extern __shared__ __align__(128) unsigned char smem[];
+  T* Bs = reinterpret_cast<T*>(smem);
+  const int M = p.M, N = p.N, np = p.np, gn = p.gn;
+  for (int e = threadIdx.x; e < M * np; e += NT) {
+    int m = e / np, n = e - m * np;
+    Bs[e] = (n < N) ? p.B[(int64_t)n * p.ldb + m] : tzero<T>();
+  }
+  __syncthreads();
+
+  const int RS = NT / gn;  // rows per CTA step (gn divides 32, so NT % gn == 0)
+  const int cell = threadIdx.x % gn, rs = threadIdx.x / gn;
+  const int n0 = cell * TN;
+  for (int64_t base = (int64_t)blockIdx.x * RS; base < p.K; base += (int64_t)gridDim.x * RS) {
+    const int64_t r = base + rs;
+    const bool valid = r < p.K;
+    Acc acc[TN];
+#pragma unroll
+    for (int u = 0; u < TN; u++) acc[u] = O::zero();
+    if (valid) {
+      const T* a_row = p.A + r * p.lda;
+#pragma unroll 4
+      for (int m = 0; m < M; m++) {
+        const T a = a_row[m];
+        const T* b = Bs + m * np + n0;
+#pragma unroll
+        for (int u = 0; u < TN; u++) acc[u] = O::mac(acc[u], a, b[u]);
+      }
+    }
+    __syncwarp();  // the whole row has been read before any of it is overwritten (in place)
+    if (valid) {
+      T* c_row = p.C + r * p.ldc;
+#pragma unroll
+      for (int u = 0; u < TN; u++) {
+        const int n = n0 + u;
+        if (n < N) c_row[n] = O::finish(acc[u], p.alpha, p.beta, p.beta_zero != 0, c_row + n);
+      }
+    }
+  }
+}
+
+}  // namespace skinny
