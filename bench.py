@@ -1,0 +1,467 @@
+"""Benchmark of the tall-skinny products on GB300, in the measurement contract of this repository.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Default workload "tsmm-sweep" (the configuration the reference's GB/s-vs-M=N metric is quoted on):
+TSMM C(KxN) = alpha A(KxM) B(MxN) + beta C with alpha = 1, beta = 0.5, FP64 and complex FP64,
+M = N in {1,2,4,8,16,32,64} plus (M,N) in {(4,16),(16,4),(8,32)}, K chosen so A is 1 GiB, plus the
+in-place form (C = A) for every M = N; entries U[-1,1) from a seeded generator.  One step runs every
+shape once.  Each shape's operands are larger than L2 (129 MB), so no L2 flush is needed.
+
+Other workloads: "tsmttsm-c1" (TSMTTSM FP64 8x8, K = 2^20, 16 rotating input copies).
+
+Byte and flop formulas follow the reference's perf harness (perf.cu:208-232):
+  TSMM beta != 0: (M K + 2 N K + M N) s bytes, in place (M K + N K + M N) s; flops (MNK + NK) f
+  TSMTTSM: (M + N) K s bytes ((M K) s for Gram); flops M N K f;  f = 2 real, 8 complex.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TSMTTSM/TSMM GB/s,%roofline vs M=N; split-vs-FP64 & served p99 at ≤1e-14 err"
+SWEEP = [(1, 1), (2, 2), (4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (4, 16), (16, 4), (8, 32)]
+FALLBACK_HBM_GBS = 6800.0
+# FP64 FMA peak of this GB300 measured with a DFMA throughput loop (2 flops per FMA): 595 G FMA/s.
+FP64_PEAK_TFLOPS = 1.19
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -------------------------------------------------------------------------------- workloads
+def tsmm_bytes(M, N, K, s, inplace):
+    return (M * K + (1 if inplace else 2) * N * K + M * N) * s
+
+
+def sweep_items(include_c64=True):
+    items = []
+    for dt in (["f64", "c64"] if include_c64 else ["f64"]):
+        s = 8 if dt == "f64" else 16
+        for (M, N) in SWEEP:
+            K = (1 << 30) // (s * M)
+            items.append(dict(op="tsmm", dt=dt, M=M, N=N, K=K, inplace=False, s=s))
+    for (M, N) in SWEEP:
+        if M == N:
+            K = (1 << 30) // (8 * M)
+            items.append(dict(op="tsmm", dt="f64", M=M, N=N, K=K, inplace=True, s=8))
+    for it in items:
+        f = 8 if it["dt"] == "c64" else 2
+        it["bytes"] = tsmm_bytes(it["M"], it["N"], it["K"], it["s"], it["inplace"])
+        it["flops"] = (it["M"] * it["N"] * it["K"] + it["N"] * it["K"]) * f
+    return items
+
+
+def c1_items():
+    M = N = 8
+    K = 1 << 20
+    return [dict(op="tsmttsm", dt="f64", M=M, N=N, K=K, inplace=False, s=8, bytes=(M + N) * K * 8,
+                 flops=2 * M * N * K, copies=16)]
+
+
+def probe_tsmm_items():
+    M = N = 8
+    K = 1 << 22
+    it = dict(op="tsmm", dt="f64", M=M, N=N, K=K, inplace=False, s=8)
+    it["bytes"] = tsmm_bytes(M, N, K, 8, False)
+    it["flops"] = (M * N * K + N * K) * 2
+    return [it]
+
+
+def probe_tsmttsm_items():
+    M = N = 8
+    K = 1 << 22
+    return [dict(op="tsmttsm", dt="f64", M=M, N=N, K=K, inplace=False, s=8, bytes=(M + N) * K * 8,
+                 flops=2 * M * N * K, copies=1)]
+
+
+WORKLOADS = {
+    "probe-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22 (256 MiB A), alpha 1, beta 0.5: small case for ncu"),
+    "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),
+    "tsmm-sweep": (sweep_items, "TSMM FP64 + complex FP64, alpha 1, beta 0.5, A = 1 GiB per shape, "
+                   "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
+    "tsmttsm-c1": (c1_items, "TSMTTSM FP64 C(8x8) = A^T B, K = 2^20, alpha 1, beta 0, "
+                   "16 rotating input copies (2 GiB > L2)"),
+}
+
+
+def torch_dtype(dt):
+    import torch
+    return {"f64": torch.float64, "c64": torch.complex128, "f32": torch.float32}[dt]
+
+
+def make_operands(it, device, seed):
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    tdt = torch_dtype(it["dt"])
+
+    def u(n):
+        if tdt.is_complex:
+            r = torch.rand(2 * n, dtype=torch.float64, device=device, generator=g) * 2 - 1
+            return torch.view_as_complex(r.view(n, 2))
+        return torch.rand(n, dtype=tdt, device=device, generator=g) * 2 - 1
+
+    M, N, K = it["M"], it["N"], it["K"]
+    if it["op"] == "tsmm":
+        A = u(K * M)
+        B = u(M * N)
+        C = A if it["inplace"] else u(K * N)
+        return dict(A=[A], B=[B], C=C)
+    copies = it.get("copies", 1)
+    return dict(A=[u(K * M) for _ in range(copies)], B=[u(K * N) for _ in range(copies)],
+                C=torch.zeros(M * N, dtype=tdt, device=device))
+
+
+def call(h, it, ops, i, method):
+    M, N, K = it["M"], it["N"], it["K"]
+    acc = method if it["dt"] == "f64" else "native"
+    if it["op"] == "tsmm":
+        ld_c = M if it["inplace"] else N
+        h.tsmm(M, N, K, ops["A"][0], M, 1.0, ops["B"][0], M, 0.5, ops["C"], ld_c, acc=acc)
+    else:
+        j = i % len(ops["A"])
+        h.tsmttsm(M, N, K, ops["A"][j], M, 1.0, ops["B"][j], N, 0.0, ops["C"], M, acc=acc)
+
+
+# ------------------------------------------------------------------------------ CPU baseline
+def cpu_sample(items, seconds_budget=12.0):
+    """Times the oracle's OpenMP loops (the reference harness's loop form) on a row sample of each
+    shape; returns (GB/s, cores, description)."""
+    import numpy as np
+    from oracle import oracle as O
+    rng = np.random.default_rng(1)
+    cores = O.max_threads()
+    tot_b, tot_t = 0.0, 0.0
+    frac = 1 / 16
+    for it in items:
+        M, N = it["M"], it["N"]
+        Ks = max(1024, int(it["K"] * frac))
+        npdt = np.complex128 if it["dt"] == "c64" else np.float64
+        def u(n):
+            if npdt == np.complex128:
+                return rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+            return rng.uniform(-1, 1, n)
+        A, B = u(Ks * M), u((M * N) if it["op"] == "tsmm" else Ks * N)
+        if it["op"] == "tsmm":
+            C = A if it["inplace"] else u(Ks * N)
+            t0 = time.perf_counter()
+            O.tsmm(M, N, Ks, A, M, 1.0, B, M, 0.5, C, M if it["inplace"] else N)
+            dt = time.perf_counter() - t0
+            tot_b += tsmm_bytes(M, N, Ks, it["s"], it["inplace"])
+        else:
+            C = np.zeros(M * N, dtype=npdt)
+            t0 = time.perf_counter()
+            O.tsmttsm(M, N, Ks, A, M, 1.0, B, N, 0.0, C, M)
+            dt = time.perf_counter() - t0
+            tot_b += (M + N) * Ks * it["s"]
+        tot_t += dt
+        if tot_t > seconds_budget:
+            break
+    return tot_b / tot_t / 1e9, cores, f"oracle OpenMP loops on every shape with K/16 rows (>=1024), {cores} threads"
+
+
+# ------------------------------------------------------------------------------------- main
+def dist_setup(n_gpus):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args):
+    """The reference arm: the reference has no CPU implementation of its products (its own oracle
+    is cuBLAS), so this arm times the oracle port of its loops on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    items = WORKLOADS[args.workload][0]()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(items[:1], 2.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, cores, desc = cpu_sample(items, seconds_budget=max(2.0, 60.0 / max(1, args.steps)))
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    v = sum(vals) / len(vals)
+    line = {"metric": METRIC, "value": round(v, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic U[-1,1) seeded",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload][1]},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tsmm-sweep", choices=sorted(WORKLOADS))
+    ap.add_argument("--method", default="auto", choices=["auto", "native", "split", "dd"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from skinny_matmul_gb300 import Handle, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    items = WORKLOADS[args.workload][0]()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ops = [make_operands(it, dev, 1000 + i + 77 * rank) for i, it in enumerate(items)]
+    torch.cuda.synchronize()
+
+    def step(i, events=None):
+        for j, (it, op) in enumerate(zip(items, ops)):
+            if events is not None:
+                events[j][0].record()
+            call(h, it, op, i, args.method)
+            if events is not None:
+                events[j][1].record()
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    h.check_device()
+
+    # ---- timed region: K steps, barrier + synchronize on both sides, CUDA events per launch
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in items]
+          for _ in range(args.steps)]
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = L.skinny_kernel_launches()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e_start.record()
+        for i in range(args.steps):
+            step(i, ev[i])
+        e_end.record()
+        torch.cuda.synchronize()
+    barrier(world)
+    launches = L.skinny_kernel_launches() - n0
+    total_ms = e_start.elapsed_time(e_end)
+    total_ms = max_over_ranks(total_ms, world)
+    bytes_step = sum(it["bytes"] for it in items)
+    flops_step = sum(it["flops"] for it in items)
+    all_bytes = sum_over_ranks(bytes_step * args.steps, world)
+    value = all_bytes / (total_ms * 1e-3) / 1e9
+    hbm, peak_kind = peaks()
+
+    # per-shape table and the dominant kernel's roofline (sum over its launches)
+    per = []
+    kern_ms = 0.0
+    for j, it in enumerate(items):
+        ts = sorted(ev[i][j][0].elapsed_time(ev[i][j][1]) for i in range(args.steps))
+        t = ts[len(ts) // 2] * 1e-3
+        kern_ms += sum(ev[i][j][0].elapsed_time(ev[i][j][1]) for i in range(args.steps))
+        gbs = it["bytes"] / t / 1e9
+        tf = it["flops"] / t / 1e12
+        per.append({"op": it["op"], "dtype": it["dt"], "M": it["M"], "N": it["N"], "K": it["K"],
+                    "inplace": it["inplace"], "us": round(t * 1e6, 1), "GB/s": round(gbs, 1),
+                    "hbm_frac": round(gbs / hbm, 4), "TFLOP/s": round(tf, 3),
+                    "fp64_frac": round(tf / (FP64_PEAK_TFLOPS * (1 if it["dt"] != "c64" else 1)), 4)})
+    achieved = bytes_step * args.steps / (kern_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get(args.workload),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "kernel": "tsmm_kernel" if items[0]["op"] == "tsmm" else "tsmttsm_kernel",
+                "fp64_tflops": round(flops_step * args.steps / (kern_ms * 1e-3) / 1e12, 3),
+                "fp64_peak_tflops_measured": FP64_PEAK_TFLOPS}
+
+    # ---- end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(h, items, ops, args, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, desc = cpu_sample(items)
+        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic U[-1,1) from a seeded generator",
+                "config": {"workload": args.workload, "description": WORKLOADS[args.workload][1],
+                           "method_fp64": args.method, "l2": "operands larger than L2 (no flush needed)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk.summary(), "sweep": per}
+        print(json.dumps(line), flush=True)
+    h.check_device()
+    h.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# DRAM bytes per step of the dominant kernel from one ncu capture (profiles/), or None.
+TRAFFIC = {}
+
+
+def measure_e2e(h, items, ops, args, world):
+    """Same metric through the public API with HOST buffers: every step copies each shape's inputs
+    from pinned host memory to the device, runs the product and copies the result back."""
+    import torch
+    maxA = max(o["A"][0].numel() * o["A"][0].element_size() for o in ops)
+    maxB = max(o["B"][0].numel() * o["B"][0].element_size() for o in ops)
+    maxC = max(o["C"].numel() * o["C"].element_size() for o in ops)
+    hA = torch.empty(maxA, dtype=torch.uint8, pin_memory=True)
+    hB = torch.empty(maxB, dtype=torch.uint8, pin_memory=True)
+    hC = torch.empty(maxC, dtype=torch.uint8, pin_memory=True)
+    # host values must be finite numbers: fill as uniform doubles
+    for t in (hA, hB, hC):
+        d = t.view(torch.float64)
+        d.uniform_(-1, 1)
+    steps = max(1, min(args.steps, 3))
+
+    def as_bytes(t):
+        return (torch.view_as_real(t) if t.is_complex() else t).view(torch.uint8)
+
+    h2d = d2h = 0
+
+    def one():
+        nonlocal h2d, d2h
+        h2d = d2h = 0
+        for it, op in zip(items, ops):
+            A, B, C = op["A"][0], op["B"][0], op["C"]
+            nA, nB, nC = (x.numel() * x.element_size() for x in (A, B, C))
+            as_bytes(A).view(-1).copy_(hA[:nA], non_blocking=True)
+            as_bytes(B).view(-1).copy_(hB[:nB], non_blocking=True)
+            h2d += nA + nB
+            if it["op"] == "tsmm" and not it["inplace"]:
+                as_bytes(C).view(-1).copy_(hC[:nC], non_blocking=True)
+                h2d += nC
+            call(h, it, op, 0, args.method)
+            hC[:nC].copy_(as_bytes(C).view(-1), non_blocking=True)
+            d2h += nC
+    one()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        one()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
+    b = sum_over_ranks(sum(it["bytes"] for it in items) * steps, world)
+    return {"value": round(b / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": steps}
+
+
+if __name__ == "__main__":
+    main()

@@ -81,6 +81,10 @@ const char* skinny_last_error(void);
  * the last check (the flag is then cleared and the handle's workspaces are reset). */
 skinny_status skinny_check_device(skinny_handle handle);
 
+/* Number of kernels this library has launched in this process (all devices, all handles);
+ * lets a caller count device launches inside a timed region.  No counterpart in the reference. */
+uint64_t skinny_kernel_launches(void);
+
 /* TSMTTSM, replaces tsmttsm/genv{3,3x,5,6,7,8}.cuh, specsmall.cuh (+ their deviceReduce) and
  * tsmttsm/gen_cublas.cuh:12-46.  alpha/beta point to one HOST value of the dtype. */
 skinny_status skinny_tsmttsm(skinny_handle handle, skinny_dtype dtype, skinny_acc acc, int64_t M,

@@ -1,6 +1,7 @@
 // api.cu -- the C ABI (include/skinny.h): handles, workspaces, argument checks, dispatch.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <climits>
 #include <cstring>
 #include <map>
@@ -14,6 +15,8 @@ namespace skinny {
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
+static std::atomic<uint64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 skinny_status workspace_ensure(Workspace& ws, size_t bytes, cudaStream_t st) {
   if (!ws.counter) {
@@ -137,6 +140,8 @@ extern "C" const char* skinny_status_string(skinny_status s) {
 }
 
 extern "C" const char* skinny_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" uint64_t skinny_kernel_launches(void) { return g_launches.load(); }
 
 extern "C" skinny_status skinny_check_device(skinny_handle h) {
   if (!h) return SKINNY_BAD_ARG;

@@ -33,6 +33,8 @@ struct Workspace {
 // the old buffer) and make sure the ticket counter exists and is zero.
 skinny_status workspace_ensure(Workspace& ws, size_t bytes, cudaStream_t stream);
 void set_error(const std::string& msg);
+// Counts every kernel launch of the library (skinny_kernel_launches()).
+void count_launch();
 
 // Launch options chosen by the caller (autotuner / request loop).  0 = default.
 struct LaunchOpts {
@@ -63,6 +65,7 @@ skinny_status tsmttsm_launch_tile(const TsmttsmArgs<T>& a, dim3 grid, int smem, 
   auto kern = tsmttsm_kernel<T, Acc, TM, TN>;
   ensure_smem_attr(kern, smem, attr);
   kern<<<grid, TSMTTSM_THREADS, smem, st>>>(a);
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("tsmttsm launch: ") + cudaGetErrorString(e));
@@ -215,6 +218,7 @@ skinny_status tsmm_launch_tile(const TsmmArgs<T>& a, int bps, int sms, int smem,
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
   kern<<<(int)grid, TSMM_THREADS, smem, st>>>(a);
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("tsmm launch: ") + cudaGetErrorString(e));

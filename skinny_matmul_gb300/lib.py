@@ -52,6 +52,7 @@ SIGNATURES = {
     "skinny_status_string": (ctypes.c_char_p, [_i]),
     "skinny_last_error": (ctypes.c_char_p, []),
     "skinny_check_device": (_i, [_vp]),
+    "skinny_kernel_launches": (ctypes.c_uint64, []),
     "skinny_tsmttsm": (_i, _PROD),
     "skinny_tsmm": (_i, _PROD),
     "skinny_svqb": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
