@@ -110,6 +110,23 @@ skinny_status skinny_tsmm(skinny_handle handle, skinny_dtype dtype, skinny_acc a
 skinny_status skinny_svqb(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M,
                           double* X, int64_t ldx, double* orth_err_out, void* stream);
 
+/* FP64 TSMTTSM that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code that runs under an allocator owning the whole
+ * device pool, or a latency-critical path where cudaMalloc's implicit device synchronisation is
+ * not allowed, cannot create a skinny_handle (whose workspaces are cudaMalloc'ed).  This entry
+ * point runs the FP64 TSMTTSM kernel with its scratch in a fixed 16 MiB device array inside the
+ * library (held by every GPU that loads the library until the process exits); A, B and C are
+ * still the caller's.  It uses the current device and the given stream.
+ *   - The first call on a device looks up the array's device address; make it before any stream
+ *     capture.
+ *   - M*N*8 bytes of partial sums per CTA must fit in 16 MiB: M*N <= 2097152, else
+ *     SKINNY_BAD_ARG; for large M*N the grid is reduced so the partials fit.
+ *   - Every call shares the one array (the counters are cleared on the stream at each call):
+ *     calls that overlap on the GPU race and must be ordered by the caller. */
+skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K, const double* A,
+                                      int64_t lda, double alpha, const double* B, int64_t ldb,
+                                      double beta, double* C, int64_t ldc, void* stream);
+
 /* ---- Reference-shaped entry points ---------------------------------------------------------
  * Exactly MatmulFunctionType (versions.hpp:43-45).  They run on the legacy default stream with a
  * per-device default handle, like the reference's launchers (e.g. tsmttsm/genv5.cuh:93-114,

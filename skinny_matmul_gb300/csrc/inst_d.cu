@@ -10,3 +10,12 @@ template skinny_status tsmm_run<double, double>(const DeviceInfo&, cudaStream_t,
                                        const double*, int64_t, double, const double*, int64_t, double, bool, double*,
                                        int64_t, const LaunchOpts&);
 }  // namespace skinny
+
+namespace skinny {
+// used by the allocation-free entry point in static_scratch.cu
+template skinny_status tsmttsm_plan<double, double>(const DeviceInfo&, int64_t, int64_t, int64_t,
+                                                    const void*, int64_t, const void*, int64_t, bool,
+                                                    const LaunchOpts&, TsmttsmPlan&);
+template skinny_status tsmttsm_dispatch<double, double>(int, int, const TsmttsmArgs<double>&, dim3,
+                                                        int, cudaStream_t);
+}  // namespace skinny

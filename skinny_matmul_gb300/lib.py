@@ -56,6 +56,8 @@ SIGNATURES = {
     "skinny_tsmttsm": (_i, _PROD),
     "skinny_tsmm": (_i, _PROD),
     "skinny_svqb": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "skinny_tsmttsm_d_static": (_i, [_i64, _i64, _i64, _vp, _i64, ctypes.c_double, _vp, _i64,
+                                     ctypes.c_double, _vp, _i64, _vp]),
     "skinny_tsmttsm_s": (_i, _ref_sig(ctypes.c_float, ctypes.c_float)),
     "skinny_tsmttsm_d": (_i, _ref_sig(ctypes.c_double, ctypes.c_double)),
     "skinny_tsmttsm_c": (_i, _ref_sig(c32, c32)),
