@@ -1,0 +1,119 @@
+"""GPU parity tests of the FP64 split-precision TSMTTSM (tcgen05 tensor cores) against the oracle.
+
+Bars: golden integer cases bit-exact; random data within the FP64 bound 8 sqrt(K) 2^-53 normwise
+against the exact oracle and, for the wide-exponent workload (s * 2^e, e in [-20, 20]), within
+1e-15 normwise; results independent of the launch (deterministic).
+"""
+import numpy as np
+import pytest
+
+import common
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+SPLIT_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and not c["cplx"] and c["M"] <= 16 and c["N"] <= 16]
+
+
+@pytest.mark.parametrize("case", SPLIT_CASES, ids=lambda c: c["id"])
+def test_split_golden_integer_cases_bit_exact(handle, case):
+    c = case
+    A, B, C = dev(c["A"]), dev(c["B"]), dev(c["C"])
+    if c["self"]:
+        B = A
+    handle.tsmttsm(c["M"], c["N"], c["K"], A, c["lda"], 1.0, B, c["ldb"], float(c["beta"]), C, c["ldc"], acc="split")
+    assert np.array_equal(host(C), c["exp"])
+
+
+SHAPES = [(1, 1, 1000), (2, 2, 70000), (4, 4, 33333), (8, 8, 1 << 20), (16, 16, 100000), (4, 16, 12345),
+          (16, 4, 12345), (5, 3, 1001), (13, 7, 4096), (8, 8, 127), (8, 8, 129), (3, 3, 1)]
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_split_uniform_vs_exact(handle, M, N, K):
+    rng = np.random.default_rng(M * 31 + N * 7 + K)
+    lda, ldb, ldc = M, N, M + 2
+    A = rng.uniform(-1, 1, K * lda)
+    B = rng.uniform(-1, 1, K * ldb)
+    C0 = rng.uniform(-1, 1, N * ldc)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), lda, 1.25, dev(B), ldb, -0.5, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, N, K, A, lda, B, ldb, C0, ldc, 1.25, -0.5)
+    err = common.normwise(got, exp, den, common.c_mask_tsmttsm(M, N, ldc))
+    assert err <= common.tol(np.float64, K), err
+    assert err <= 4e-16, err  # the split sum is formed exactly per period; only FP64 window sums round
+
+
+@pytest.mark.parametrize("M", [8, 16])
+def test_split_wide_exponents_c3_distribution(handle, M):
+    """Entries s * 2^e, s in U[1,2), random sign, e in [-20, 20] (the precision workload)."""
+    rng = np.random.default_rng(100 + M)
+    K = 1 << 17
+    A = common.spread(rng, K * M)
+    B = common.spread(rng, K * M)
+    Cd = dev(np.zeros(M * M))
+    handle.tsmttsm(M, M, K, dev(A), M, 1.0, dev(B), M, 0.0, Cd, M, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, M, K, A, M, B, M, np.zeros(M * M), M, 1.0, 0.0)
+    err = common.normwise(got, exp, den)
+    assert err <= 1e-15, err
+    # the CUDA-core FP64 result for comparison: the split result is at least as accurate
+    Cp = dev(np.zeros(M * M))
+    handle.tsmttsm(M, M, K, dev(A), M, 1.0, dev(B), M, 0.0, Cp, M, acc="native")
+    assert err <= 2 * common.normwise(host(Cp), exp, den) + 1e-17
+
+
+def test_split_gram_and_growing_exponents(handle):
+    """Gram mode, with row magnitudes growing along K so column exponents rise mid-stream and
+    force new accumulation periods."""
+    rng = np.random.default_rng(5)
+    M, K = 12, 200003
+    scale = np.ldexp(1.0, (np.arange(K) // 5000) - 20)
+    X = (rng.uniform(-1, 1, (K, M)) * scale[:, None]).ravel()
+    Sd = dev(np.zeros(M * M))
+    Xd = dev(X)
+    handle.tsmttsm(M, M, K, Xd, M, 1.0, Xd, M, 0.0, Sd, M, acc="split")
+    got = host(Sd)
+    exp, den = common.tsmttsm_expected(M, M, K, X, M, X, M, np.zeros(M * M), M, 1.0, 0.0)
+    assert common.normwise(got, exp, den) <= 4e-16
+
+
+def test_split_unaligned_padded_and_zero_columns(handle):
+    rng = np.random.default_rng(8)
+    M, N, K = 8, 6, 50001
+    lda, ldb = M + 3, N + 1
+    A = rng.uniform(-1, 1, K * lda + 1)
+    B = rng.uniform(-1, 1, K * ldb + 1)
+    A.reshape(-1)[1:][: K * lda].reshape(K, lda)[:, 2] = 0.0  # an all-zero column
+    Ad, Bd = dev(A), dev(B)
+    for off in (0, 1):
+        Cd = dev(np.zeros(N * M))
+        handle.tsmttsm(M, N, K, Ad[off:], lda, 1.0, Bd[off:], ldb, 0.0, Cd, M, acc="split")
+        exp, den = common.tsmttsm_expected(M, N, K, A[off:].copy(), lda, B[off:].copy(), ldb, np.zeros(M * N), M,
+                                           1.0, 0.0)
+        assert common.normwise(host(Cd), exp, den) <= 4e-16, off
+
+
+def test_split_deterministic_and_auto(handle):
+    rng = np.random.default_rng(2)
+    M = N = 8
+    K = 1 << 20
+    A, B = dev(rng.uniform(-1, 1, K * M)), dev(rng.uniform(-1, 1, K * N))
+    outs = []
+    for acc in ("split", "split", "auto"):
+        Cd = dev(np.zeros(M * N))
+        handle.tsmttsm(M, N, K, A, M, 1.0, B, N, 0.0, Cd, M, acc=acc)
+        outs.append(host(Cd))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    handle.check_device()
