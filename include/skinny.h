@@ -127,6 +127,68 @@ skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K, const dou
                                       int64_t lda, double alpha, const double* B, int64_t ldb,
                                       double beta, double* C, int64_t ldc, void* stream);
 
+/* Autotuner.  Replaces the reference's compile-time choice of one kernel variant per (M, N)
+ * (versions.hpp:48-177, multi_dispatch.cuh, tsmm/fix_blend.cuh:7-29): for (op, dtype, acc, M, N)
+ * it times the candidate launch shapes (CTAs per SM, rows per tile) and, for SKINNY_ACC_AUTO on
+ * R64, the split-precision against the CUDA-core method, on scratch operands of K rows, and
+ * records the fastest in the handle's table; later calls with that key use it.
+ * op: 0 = TSMTTSM, 1 = TSMM.  Synchronises `stream`; allocates and frees its scratch. */
+skinny_status skinny_autotune(skinny_handle handle, int op, skinny_dtype dtype, skinny_acc acc,
+                              int64_t M, int64_t N, int64_t K, void* stream);
+/* The tuned table as JSON text (buf of len bytes; *written = bytes needed incl. the NUL). */
+skinny_status skinny_tune_export(skinny_handle handle, char* buf, size_t len, size_t* written);
+/* Merge a table produced by skinny_tune_export. */
+skinny_status skinny_tune_import(skinny_handle handle, const char* json);
+
+/* ---- Request loop (continuous batching).  No counterpart in the reference.
+ * A server accepts TSMTTSM / TSMM / SVQB requests on HOST buffers as they arrive, admits them in
+ * arrival order while their device bytes fit the memory budget and an in-flight slot is free,
+ * runs each (upload, product, download) on one of its streams so that the work of requests in
+ * flight overlaps on the device, and retires them as their completion events fire; admission
+ * continues while others run.  Host buffers must stay valid until the ticket completes; pinned
+ * host memory lets uploads and downloads overlap with compute.  A server created with a NULL
+ * handle runs in dry mode: nothing touches a device and each request "runs" for a time
+ * proportional to its bytes (for testing the scheduling logic without a GPU). */
+typedef enum { SKINNY_OP_TSMTTSM = 0, SKINNY_OP_TSMM = 1, SKINNY_OP_SVQB = 2 } skinny_op;
+
+typedef struct {
+  skinny_op op;
+  skinny_dtype dtype;
+  skinny_acc acc;
+  int64_t M, N, K;
+  const void* A; /* host; SVQB: X (K x M), updated in place through C */
+  int64_t lda;
+  const void* B; /* host; unused for SVQB */
+  int64_t ldb;
+  void* C;       /* host; read when beta != 0, always written; SVQB: X */
+  int64_t ldc;
+  double alpha[2], beta[2]; /* (re, im); real dtypes use [0] */
+} skinny_request;
+
+typedef struct {
+  uint64_t submitted, completed, failed, rejected;
+  double p50_latency_us, p99_latency_us, mean_latency_us;
+  double bytes; /* algorithmic bytes of the completed requests */
+  double busy_seconds; /* wall time from the first admission to the last completion */
+  uint64_t peak_bytes_in_use;
+  uint64_t max_inflight_seen;
+} skinny_server_stats;
+
+typedef struct skinny_server_st* skinny_server;
+
+skinny_status skinny_server_create(skinny_server* server, skinny_handle handle, uint64_t mem_budget_bytes,
+                                   int num_streams, int max_inflight);
+/* Queue a request; *ticket identifies it.  SKINNY_NO_MEM if it can never fit the budget. */
+skinny_status skinny_server_submit(skinny_server server, const skinny_request* request, uint64_t* ticket);
+/* SKINNY_NOT_READY while the ticket runs; otherwise SKINNY_OK with *result = the request's status. */
+skinny_status skinny_server_poll(skinny_server server, uint64_t ticket, skinny_status* result);
+/* Block until the ticket completes or timeout_s passes (SKINNY_TIMEOUT). */
+skinny_status skinny_server_wait(skinny_server server, uint64_t ticket, skinny_status* result,
+                                 double timeout_s);
+skinny_status skinny_server_drain(skinny_server server, double timeout_s);
+skinny_status skinny_server_stats_get(skinny_server server, skinny_server_stats* stats);
+skinny_status skinny_server_destroy(skinny_server server); /* drains first */
+
 /* ---- Reference-shaped entry points ---------------------------------------------------------
  * Exactly MatmulFunctionType (versions.hpp:43-45).  They run on the legacy default stream with a
  * per-device default handle, like the reference's launchers (e.g. tsmttsm/genv5.cuh:93-114,

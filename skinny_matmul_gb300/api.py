@@ -92,6 +92,24 @@ class Handle:
         return self._product(self.lib.skinny_tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc,
                              acc, stream, dtype)
 
+    def autotune(self, op, dtype, M, N, K, acc="auto", stream=None):
+        """Measure launch shapes (and, for FP64 'auto', split vs CUDA-core) for (op, dtype, acc,
+        M, N) on scratch operands of K rows; the handle then uses the fastest for that key.
+        op: 'tsmttsm' | 'tsmm'; dtype: 'float32' | 'float64' | 'complex64' | 'complex128'."""
+        code = {"float32": L.R32, "float64": L.R64, "complex64": L.C32, "complex128": L.C64}[dtype]
+        return L.check(self.lib.skinny_autotune(self.h, 0 if op == "tsmttsm" else 1, code, _ACC[acc],
+                                                M, N, K, _stream(stream)))
+
+    def tune_export(self) -> str:
+        n = ctypes.c_size_t()
+        L.check(self.lib.skinny_tune_export(self.h, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        L.check(self.lib.skinny_tune_export(self.h, buf, n.value, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def tune_import(self, text: str):
+        return L.check(self.lib.skinny_tune_import(self.h, text.encode()))
+
     def svqb(self, K, M, X, ldx, gram_acc="split", orth_err=True, stream=None):
         """In-place SVQB of X (K x M, FP64); returns ||Q^T Q - I||_F when orth_err."""
         err = ctypes.c_double(-1.0)
@@ -145,3 +163,76 @@ def launchers(op: str, dtype: str) -> List[Tuple[Callable, str]]:
                         ctypes.cast(_ptr(B), P), ldb, conv(beta), ctypes.cast(_ptr(C), P), ldc))
 
     return [(fn, f"GB300_{op.upper()}_{sfx.upper()}")]
+
+
+_OPS = {"tsmttsm": L.OP_TSMTTSM, "tsmm": L.OP_TSMM, "svqb": L.OP_SVQB}
+_DT = {"float32": L.R32, "float64": L.R64, "complex64": L.C32, "complex128": L.C64}
+
+
+class Server:
+    """Request loop with continuous batching (skinny_server_* in include/skinny.h).
+
+    Requests carry HOST numpy buffers (keep them alive until the ticket completes; pinned memory
+    overlaps transfers).  handle=None runs the scheduler in dry mode (no device work)."""
+
+    def __init__(self, handle: Handle | None, mem_budget_bytes: int, num_streams: int = 4,
+                 max_inflight: int = 16):
+        self.lib = L.load()
+        s = ctypes.c_void_p()
+        L.check(self.lib.skinny_server_create(ctypes.byref(s), handle.h if handle else None,
+                                              int(mem_budget_bytes), num_streams, max_inflight))
+        self.s = s
+        self._keep = {}
+
+    def submit(self, op, dtype, M, N, K, A, lda, B=None, ldb=0, C=None, ldc=0, alpha=1.0, beta=0.0,
+               acc="native"):
+        """Queue a request; returns its ticket.  A, B, C are host arrays (numpy) or addresses."""
+        def addr(x):
+            if x is None:
+                return None
+            if isinstance(x, int):
+                return x
+            return x.ctypes.data
+        r = L.Request()
+        r.op, r.dtype, r.acc = _OPS[op], _DT[dtype], _ACC[acc]
+        r.M, r.N, r.K = M, N, K
+        r.A, r.lda, r.B, r.ldb, r.C, r.ldc = addr(A), lda, addr(B), ldb, addr(C), ldc
+        a, b = complex(alpha), complex(beta)
+        r.alpha[0], r.alpha[1], r.beta[0], r.beta[1] = a.real, a.imag, b.real, b.imag
+        t = ctypes.c_uint64()
+        st = self.lib.skinny_server_submit(self.s, ctypes.byref(r), ctypes.byref(t))
+        if st == L.OK:
+            self._keep[t.value] = (A, B, C)
+        return st, t.value
+
+    def poll(self, ticket):
+        res = ctypes.c_int(-1)
+        st = self.lib.skinny_server_poll(self.s, ticket, ctypes.byref(res))
+        return st, res.value
+
+    def wait(self, ticket, timeout_s=60.0):
+        res = ctypes.c_int(-1)
+        st = self.lib.skinny_server_wait(self.s, ticket, ctypes.byref(res), timeout_s)
+        if st == L.OK:
+            self._keep.pop(ticket, None)
+        return st, res.value
+
+    def drain(self, timeout_s=600.0):
+        return L.check(self.lib.skinny_server_drain(self.s, timeout_s))
+
+    def stats(self) -> dict:
+        s = L.ServerStats()
+        L.check(self.lib.skinny_server_stats_get(self.s, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in L.ServerStats._fields_}
+
+    def close(self):
+        if self.s:
+            self.lib.skinny_server_destroy(self.s)
+            self.s = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -228,6 +228,8 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_R64:
       if (acc == SKINNY_ACC_DD)
         return run_t<double, dd>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+      if (acc == SKINNY_ACC_AUTO && o.method == SKINNY_ACC_NATIVE)
+        return run_t<double, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       if (acc == SKINNY_ACC_SPLIT || acc == SKINNY_ACC_AUTO) {
         skinny_status s = split_product(h, tsmm, M, N, K, (const double*)A, lda, alpha,
                                         (const double*)B, ldb, beta, (double*)C, ldc, st,

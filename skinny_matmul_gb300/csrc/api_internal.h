@@ -16,6 +16,7 @@ struct skinny_handle_st {
   std::mutex mu;                                        // guards ws / tune / extra state
   std::map<cudaStream_t, skinny::Workspace> ws;         // one partial-sum buffer per stream
   std::map<std::tuple<int, int, int, int64_t, int64_t>, skinny::LaunchOpts> tune;  // autotuner table
+  std::map<std::tuple<int, int, int, int64_t, int64_t>, float> tune_us;            // measured time
   std::vector<void*> extra_allocs;                       // buffers owned by other subsystems
   std::map<cudaStream_t, void*> split_ws;                // split-precision scratch per stream
   std::map<cudaStream_t, size_t> split_ws_bytes;

@@ -40,6 +40,7 @@ void count_launch();
 struct LaunchOpts {
   int blocks_per_sm = 0;
   int rows_per_tile = 0;
+  int method = -1;  // for SKINNY_ACC_AUTO: the method the autotuner measured fastest (-1: none)
 };
 
 inline int pow2ceil(int64_t v) {

@@ -28,6 +28,27 @@ class c64(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double)]
 
 
+class Request(ctypes.Structure):
+    """skinny_request (include/skinny.h)."""
+    _fields_ = [("op", ctypes.c_int), ("dtype", ctypes.c_int), ("acc", ctypes.c_int),
+                ("M", ctypes.c_int64), ("N", ctypes.c_int64), ("K", ctypes.c_int64),
+                ("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
+                ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64),
+                ("alpha", ctypes.c_double * 2), ("beta", ctypes.c_double * 2)]
+
+
+class ServerStats(ctypes.Structure):
+    """skinny_server_stats (include/skinny.h)."""
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64), ("p50_latency_us", ctypes.c_double),
+                ("p99_latency_us", ctypes.c_double), ("mean_latency_us", ctypes.c_double),
+                ("bytes", ctypes.c_double), ("busy_seconds", ctypes.c_double),
+                ("peak_bytes_in_use", ctypes.c_uint64), ("max_inflight_seen", ctypes.c_uint64)]
+
+
+OP_TSMTTSM, OP_TSMM, OP_SVQB = 0, 1, 2
+
+
 class SkinnyError(RuntimeError):
     def __init__(self, status: int, detail: str = ""):
         self.status = status
@@ -56,6 +77,16 @@ SIGNATURES = {
     "skinny_tsmttsm": (_i, _PROD),
     "skinny_tsmm": (_i, _PROD),
     "skinny_svqb": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "skinny_autotune": (_i, [_vp, _i, _i, _i, _i64, _i64, _i64, _vp]),
+    "skinny_tune_export": (_i, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)]),
+    "skinny_tune_import": (_i, [_vp, ctypes.c_char_p]),
+    "skinny_server_create": (_i, [ctypes.POINTER(_vp), _vp, ctypes.c_uint64, _i, _i]),
+    "skinny_server_submit": (_i, [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "skinny_server_poll": (_i, [_vp, ctypes.c_uint64, ctypes.POINTER(_i)]),
+    "skinny_server_wait": (_i, [_vp, ctypes.c_uint64, ctypes.POINTER(_i), ctypes.c_double]),
+    "skinny_server_drain": (_i, [_vp, ctypes.c_double]),
+    "skinny_server_stats_get": (_i, [_vp, ctypes.POINTER(ServerStats)]),
+    "skinny_server_destroy": (_i, [_vp]),
     "skinny_tsmttsm_d_static": (_i, [_i64, _i64, _i64, _vp, _i64, ctypes.c_double, _vp, _i64,
                                      ctypes.c_double, _vp, _i64, _vp]),
     "skinny_tsmttsm_s": (_i, _ref_sig(ctypes.c_float, ctypes.c_float)),
