@@ -151,6 +151,7 @@ def probe_split_items():
 
 
 WORKLOADS = {
+    "probe-split-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-split": (probe_split_items, "TSMTTSM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22 (256 MiB A), alpha 1, beta 0.5: small case for ncu"),
     "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),

@@ -231,9 +231,10 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
       if (acc == SKINNY_ACC_AUTO && o.method == SKINNY_ACC_NATIVE)
         return run_t<double, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       if (acc == SKINNY_ACC_SPLIT || acc == SKINNY_ACC_AUTO) {
+        // a tuned SPLIT entry forces the split kernel; otherwise AUTO uses its measured heuristic
         skinny_status s = split_product(h, tsmm, M, N, K, (const double*)A, lda, alpha,
                                         (const double*)B, ldb, beta, (double*)C, ldc, st,
-                                        acc == SKINNY_ACC_AUTO);
+                                        acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_SPLIT);
         if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
       }
       return run_t<double, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
@@ -242,6 +243,11 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
         return run_t<c32, c32>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
     case SKINNY_C64:
+      if (tsmm && (acc == SKINNY_ACC_SPLIT || (acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_NATIVE))) {
+        skinny_status s = split_tsmm(h, true, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+                                     (double*)C, ldc, st, acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_SPLIT);
+        if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
+      }
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<c64, c64>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;

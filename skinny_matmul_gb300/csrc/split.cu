@@ -496,16 +496,15 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
                             int64_t ldb, const void* beta, double* C, int64_t ldc,
                             cudaStream_t st, bool autoselect) {
   using namespace split;
-  if (tsmm) {
-    set_error("split precision: TSMM not provided");
-    return SKINNY_UNSUPPORTED;
-  }
+  if (tsmm) return split_tsmm(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, autoselect);
   if (M > 16 || N > 16) {
     set_error("split precision TSMTTSM: M, N <= 16 in this build");
     return SKINNY_UNSUPPORTED;
   }
-  if (autoselect && K < 4096) {  // short K: the CUDA-core kernel is as fast
-    set_error("split precision: K too small for auto selection");
+  // auto selection (measured on GB300): the split kernel wins from M*N >= 256 on; below that the
+  // CUDA-core FP64 kernel is as fast or faster.  The autotuner can override per shape.
+  if (autoselect && (K < 4096 || M * N < 256)) {
+    set_error("split precision: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
   }
   Args a;

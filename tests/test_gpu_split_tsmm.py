@@ -1,0 +1,122 @@
+"""GPU parity tests of the FP64 / complex FP64 split-precision TSMM (tcgen05) against the oracle.
+
+Bars: golden integer cases bit-exact; random data within 8 sqrt(M) u normwise (u = 2^-53) of the
+exact oracle and, as the split products are formed exactly and rounded once, within 4e-16."""
+import numpy as np
+import pytest
+
+import common
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+CASES = [c for c in common.int_cases() if c["op"] == "tsmm" and
+         ((not c["cplx"] and c["M"] <= 32 and c["N"] <= 32) or (c["cplx"] and c["M"] <= 16 and c["N"] <= 16))]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["id"])
+def test_split_tsmm_golden_bit_exact(handle, case):
+    c = case
+    A, B, C = dev(c["A"]), dev(c["B"]), dev(c["C"])
+    if c["self"]:
+        A = C
+    handle.tsmm(c["M"], c["N"], c["K"], A, c["lda"], 1.0, B, c["ldb"], float(c["beta"]), C, c["ldc"], acc="split")
+    got = host(C)
+    assert np.array_equal(got, c["exp"])
+
+
+SHAPES = [(1, 1), (2, 2), (4, 4), (8, 8), (16, 16), (32, 32), (4, 16), (16, 4), (8, 32), (3, 5), (17, 9), (32, 1)]
+
+
+@pytest.mark.parametrize("M,N", SHAPES)
+@pytest.mark.parametrize("inplace", [False, True])
+def test_split_tsmm_uniform(handle, M, N, inplace):
+    if inplace and M != N:
+        pytest.skip("in place needs M == N here")
+    rng = np.random.default_rng(M * 100 + N)
+    K = 20011
+    lda, ldb, ldc = M, M + 1, N
+    if inplace:
+        lda = ldc = M
+    A = rng.uniform(-1, 1, K * lda)
+    B = rng.uniform(-1, 1, N * ldb)
+    C0 = A.copy() if inplace else rng.uniform(-1, 1, K * ldc)
+    Cd = dev(C0)
+    Ad = Cd if inplace else dev(A)
+    handle.tsmm(M, N, K, Ad, lda, 1.5, dev(B), ldb, -0.5, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, C0 if inplace else A, lda, B, ldb, C0, ldc, 1.5, -0.5)
+    err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
+    assert err <= min(common.tol(np.float64, M), 4e-16), err
+
+
+@pytest.mark.parametrize("M,N", [(1, 1), (2, 2), (4, 4), (8, 8), (16, 16), (4, 16), (16, 4), (3, 7)])
+@pytest.mark.parametrize("inplace", [False, True])
+def test_split_tsmm_complex(handle, M, N, inplace):
+    if inplace and M != N:
+        pytest.skip("in place needs M == N here")
+    rng = np.random.default_rng(7 + M * 13 + N)
+    K = 10007
+    lda, ldb, ldc = M, M, N
+    A = common.uniform(rng, K * lda, np.complex128)
+    B = common.uniform(rng, N * ldb, np.complex128)
+    C0 = A.copy() if inplace else common.uniform(rng, K * ldc, np.complex128)
+    alpha, beta = 1.0 + 0.5j, 0.5 - 0.25j
+    Cd = dev(C0)
+    Ad = Cd if inplace else dev(A)
+    handle.tsmm(M, N, K, Ad, lda, alpha, dev(B), ldb, beta, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, C0 if inplace else A, lda, B, ldb, C0, ldc, alpha, beta)
+    err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
+    assert err <= min(common.tol(np.complex128, M), 8e-16), err
+
+
+def test_split_tsmm_wide_exponents_and_zero_rows(handle):
+    rng = np.random.default_rng(3)
+    M = N = 16
+    K = 30000
+    A = common.spread(rng, K * M)
+    A[: 5 * M] = 0.0  # all-zero rows
+    B = common.spread(rng, M * N)
+    C0 = common.spread(rng, K * N)
+    Cd = dev(C0)
+    handle.tsmm(M, N, K, dev(A), M, 1.0, dev(B), M, 0.25, Cd, N, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, A, M, B, M, C0, N, 1.0, 0.25)
+    assert common.normwise(got, exp, den) <= 4e-16
+
+
+def test_split_tsmm_unaligned_and_padded(handle):
+    rng = np.random.default_rng(4)
+    M, N, K = 8, 8, 5003
+    for lda, off in ((M + 3, 0), (M, 1), (3 * M + 20, 1)):
+        A = rng.uniform(-1, 1, K * lda + 1)
+        B = rng.uniform(-1, 1, M * N)
+        C0 = rng.uniform(-1, 1, K * N)
+        Cd = dev(C0)
+        Ad = dev(A)
+        handle.tsmm(M, N, K, Ad[off:], lda, 1.0, dev(B), M, 1.0, Cd, N, acc="split")
+        exp, den = common.tsmm_expected(M, N, K, A[off:].copy(), lda, B, M, C0, N, 1.0, 1.0)
+        assert common.normwise(host(Cd), exp, den) <= 4e-16, (lda, off)
+
+
+def test_split_tsmm_small_k(handle):
+    rng = np.random.default_rng(5)
+    for K in (1, 127, 128, 129, 255):
+        M, N = 8, 4
+        A = rng.uniform(-1, 1, K * M)
+        B = rng.uniform(-1, 1, M * N)
+        Cd = dev(np.zeros(K * N))
+        handle.tsmm(M, N, K, dev(A), M, 1.0, dev(B), M, 0.0, Cd, N, acc="split")
+        exp, den = common.tsmm_expected(M, N, K, A, M, B, M, np.zeros(K * N), N, 1.0, 0.0)
+        assert common.normwise(host(Cd), exp, den) <= 4e-16, K
