@@ -14,13 +14,16 @@
 //     with the most significant first: plane q holds digit q+1.  For level L = i+j (2..9) the
 //     product of the last (L-1) planes of A' with the first (L-1) planes of B' pairs exactly the
 //     digits with i + j = L, so one MMA chain per level gives D_L(r, n) = sum_{i+j=L} sum_m a_i b_j.
-//   * |D_L| <= 8 * MP * 2^14 <= 2^22 (MP <= 32): exact in the FP32 TMEM accumulator and exactly
-//     convertible to int32 with a float add.
-//   * Epilogue: V = sum_L D_L 2^(8(9-L)) as a 128-bit integer, rounded once to a double with
-//     integer instructions, times 2^(e_r + f_n - 2112) in the exponent field; beta*C is one FMA.
+//   * |D_L| <= 8 * MP * 2^14 <= 2^23: exact in the FP32 TMEM accumulator.
+//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers, its top 64 bits (from its
+//     own leading bit; the rest lies below 2^-62 of |V|) are rounded to a double with integer
+//     instructions and scaled by 2^(e_r + f_n - 2112) in the exponent field; beta*C is one FMA.
 //     Levels >= 10 are dropped (weight below 2^-56 of the leading level).
-//   * Tiles of 128 rows stream through a ring of FP64 tiles (1-D TMA bulk copies); the MMAs of tile
-//     t overlap the epilogue of tile t-1 (double-buffered TMEM accumulators).
+//   * Tiles of 128 rows: two threads per row read the row's FP64 values straight from global
+//     memory into registers (the next tile is prefetched while the current one is sliced); the
+//     MMAs of tile t overlap the epilogue of tile t-1 where two TMEM accumulators fit (N <= 32).
+//   * |D_L| <= 2^22 for contraction widths <= 32 (converted with a float add), <= 2^23 for 64
+//     (converted with cvt.rni); both exact.
 // Complex FP64 (interleaved) runs as the real product of doubled width: A (K x 2M), B' (2M x 2N)
 // with B'[2n][2m] = br, B'[2n][2m+1] = -bi, B'[2n+1][2m] = bi, B'[2n+1][2m+1] = br, C (K x 2N).
 // Inputs must be finite.
@@ -37,24 +40,21 @@ constexpr int ROWS = 128;
 constexpr int THREADS = 256;
 constexpr int DIGITS = 8;
 constexpr int HDR = 4096;      // barriers, TMEM slot, row/column exponents
-constexpr int BAL = 8192;      // alpha*B staging (<= 32 x 32 doubles)
 
 struct Args {
   const double* A;
   const double* B;  // real: B[n*ldb+m]; complex: the complex B (interleaved)
   double* C;
-  int64_t K, lda, ldb, ldc;  // in doubles (complex: already doubled)
+  int64_t K, lda, ldb, ldc;  // in doubles (complex: lda, ldc already doubled; ldb in complex elements)
   int M, N;                  // real widths (complex: 2M, 2N)
-  int MP, NM;                // padded contraction width (16 or 32), MMA N (16 or 32)
+  int NM;                    // MMA N: 16, 32 or 64
   int cplx;                  // B is complex (alpha, beta complex)
   double alpha[2], beta[2];
-  int beta_zero, inplace, bulk, stages;
+  int beta_zero, inplace, vec;  // vec: rows of A may be read as 16-byte pairs
   int64_t ntiles;
-  uint32_t tile_bytes;  // FP64 stage bytes
-  int64_t lda_s;        // row stride of the FP64 stage tile
-  int wload;            // columns staged by plain loads (in place: max(M, N), beta*C reads them)
-  uint32_t abuf;        // bytes of one A' buffer
-  int nabuf;            // A' buffers (1 or 2)
+  uint32_t abuf;  // bytes of one A' buffer
+  int nabuf;      // A' buffers (1 or 2)
+  int ntbuf;      // TMEM accumulator buffers (1 or 2)
   int tmem_cols;
   int* err;
 };
@@ -121,71 +121,67 @@ __device__ __forceinline__ uint32_t kmaj(int row, int koct, uint32_t lbo) {
   return (uint32_t)koct * lbo + (uint32_t)(row >> 3) * 128u + (uint32_t)(row & 7) * 16u;
 }
 
-// round the signed 128-bit integer (hi:lo) to the nearest double and scale by 2^E (E applied to
-// the exponent field; results are assumed to stay in the normal range)
-__device__ __forceinline__ double i128_to_double(long long hi, unsigned long long lo, int E) {
-  const bool neg = hi < 0;
-  unsigned long long h = (unsigned long long)hi, l = lo;
-  if (neg) {  // two's complement negate
-    l = ~l + 1ull;
-    h = ~h + (l == 0ull ? 1ull : 0ull);
-  }
-  if ((h | l) == 0ull) return 0.0;
-  int P;  // position of the leading one
-  unsigned long long top;  // 64 bits starting at the leading one
-  bool sticky;
-  if (h) {
-    const int z = __clzll((long long)h);
-    P = 127 - z;
-    top = z ? ((h << z) | (l >> (64 - z))) : h;
-    sticky = z ? ((l << z) != 0ull) : (l != 0ull);
-  } else {
-    const int z = __clzll((long long)l);
-    P = 63 - z;
-    top = l << z;
-    sticky = false;
-  }
-  unsigned long long mant = top >> 11;  // 53 bits
-  const unsigned long long rem = top & 0x7FFull;
-  sticky = sticky || ((rem & 0x3FFull) != 0ull);
-  const bool half = (rem & 0x400ull) != 0ull;
-  if (half && (sticky || (mant & 1ull))) mant++;
-  int ex = P + E;
-  if (mant >> 53) {
-    mant >>= 1;
-    ex++;
-  }
-  const long long bits = ((long long)(ex + 1023) << 52) | (long long)(mant & 0xFFFFFFFFFFFFFull);
-  const double v = __longlong_as_double(bits);
-  return neg ? -v : v;
+// value of (alpha * B) at (m, n) in the real view, 0 outside M x N
+__device__ __forceinline__ double alpha_b(const Args& p, int m, int n) {
+  if (m >= p.M || n >= p.N) return 0.0;
+  if (!p.cplx) return p.B[(int64_t)n * p.ldb + m] * p.alpha[0];
+  const int nc = n >> 1, mc = m >> 1;
+  const double br = p.B[2 * ((int64_t)nc * p.ldb + mc)], bi = p.B[2 * ((int64_t)nc * p.ldb + mc) + 1];
+  const double ar = br * p.alpha[0] - bi * p.alpha[1], ai = br * p.alpha[1] + bi * p.alpha[0];
+  return ((n & 1) == 0) ? ((m & 1) == 0 ? ar : -ai) : ((m & 1) == 0 ? ai : ar);
 }
 
+// A row values of this thread's half of the columns (MP/2 values) for tile row r0 + row
+template <int HALF>
+__device__ __forceinline__ void load_row(const Args& p, int64_t r0, int row, int rows, int m0, double (&v)[HALF]) {
+  const bool ok = row < rows;
+  const double* a = p.A + (r0 + row) * p.lda + m0;
+  if (ok && p.vec && m0 + HALF <= p.M) {
+#pragma unroll
+    for (int j = 0; j < HALF; j += 2) {
+      double2 x = p.inplace ? *reinterpret_cast<const double2*>(a + j) : __ldg(reinterpret_cast<const double2*>(a + j));
+      v[j] = x.x;
+      v[j + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < HALF; j++) v[j] = (ok && m0 + j < p.M) ? a[j] : 0.0;
+  }
+}
+
+// x * 2^E for a signed 64-bit integer x, rounded to 53 bits (ties away from zero); |x| < 2^63.
+__device__ __forceinline__ double i64_to_double(long long x, int E) {
+  if (x == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)x & 0x8000000000000000ull;
+  unsigned long long m = (unsigned long long)(x < 0 ? -x : x);
+  const int z = __clzll((long long)m);  // >= 1
+  m <<= z;                              // leading one at bit 63
+  unsigned long long mant = (m + 0x400ull) >> 11;  // round on bit 10; may carry to 2^53
+  int ex = 63 - z + E;
+  const unsigned long long carry = mant >> 53;
+  mant >>= carry;
+  ex += (int)carry;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+template <int MP>
 __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
+  constexpr int HALF = MP / 2;  // columns sliced per thread (two threads per row)
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bar_tma = reinterpret_cast<uint64_t*>(smem);        // [4]
   uint64_t* bar_mma = reinterpret_cast<uint64_t*>(smem + 32);   // [2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
-  int* erow = reinterpret_cast<int*>(smem + 128);               // [2][2][ROWS]: tile parity, half
-  int* fcol = reinterpret_cast<int*>(smem + 128 + 4 * ROWS * 4);  // [32]
-  const int M = p.M, N = p.N, MP = p.MP, NM = p.NM;
+  int* erow = reinterpret_cast<int*>(smem + 128);               // [2 parity][2 halves][ROWS]
+  int* fcol = reinterpret_cast<int*>(smem + 128 + 4 * ROWS * 4);  // [64]
+  const int M = p.M, N = p.N, NM = p.NM;
   const uint32_t lbo_a = ROWS * 16, lbo_b = (uint32_t)NM * 16;
-  unsigned char* bdig = smem + HDR + BAL;                         // B' (NM x 8*MP), 1024-aligned
+  unsigned char* bdig = smem + HDR;                               // B' (NM x 8*MP), 1024-aligned
   const uint32_t bdig_bytes = (uint32_t)(8 * MP / 8) * lbo_b;
   unsigned char* adig = bdig + ((bdig_bytes + 1023) & ~1023u);   // A' buffers
-  unsigned char* ring = adig + (size_t)p.nabuf * p.abuf;
-  double* bal = reinterpret_cast<double*>(smem + HDR);           // alpha*B as [m][n]
-  auto tile = [&](int s) { return reinterpret_cast<double*>(ring + (size_t)s * p.tile_bytes); };
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t t_begin = p.ntiles * blockIdx.x / gridDim.x;
   const int64_t t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const int nt = (int)(t_end - t_begin);
-  auto is_bulk = [&](int64_t t) { return p.bulk && (t + 1) * (int64_t)ROWS < p.K; };
-  auto issue = [&](int64_t t, int s) {
-    const uint32_t b = (uint32_t)(ROWS * p.lda * 8);
-    mbar_arrive_expect_tx(&bar_tma[s], b);
-    bulk_g2s(tile(s), p.A + t * ROWS * p.lda, b, &bar_tma[s]);
-  };
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -193,42 +189,23 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int s = 0; s < p.stages; s++) mbar_init(&bar_tma[s], 1);
     mbar_init(&bar_mma[0], 1);
     mbar_init(&bar_mma[1], 1);
     fence_mbar_init();
   }
-  // ---- alpha * B (FP64) as bal[m][n], column exponents, B' digits -----------------------------
-  // B' row n: plane q (digit q+1) at k = q*MP + m; entries for m >= M or n >= N are zero
-  for (int e = tid; e < MP * NM; e += THREADS) {
-    const int m = e / NM, n = e % NM;
-    double v = 0.0;
-    if (m < M && n < N) {
-      if (!p.cplx) {
-        v = p.B[(int64_t)n * p.ldb + m] * p.alpha[0];
-      } else {  // real view of complex B: (2n + s, 2m + t)
-        const int nc = n >> 1, mc = m >> 1;
-        const double br = p.B[2 * ((int64_t)nc * p.ldb + mc)], bi = p.B[2 * ((int64_t)nc * p.ldb + mc) + 1];
-        const double ar = br * p.alpha[0] - bi * p.alpha[1], ai = br * p.alpha[1] + bi * p.alpha[0];
-        v = ((n & 1) == 0) ? ((m & 1) == 0 ? ar : -ai) : ((m & 1) == 0 ? ai : ar);
-      }
-    }
-    bal[m * NM + n] = v;
-  }
-  if (tid < 32) fcol[tid] = 0;
-  __syncthreads();
+  // ---- B' = digits of alpha * B: column exponents, then (n, m-octet) units -------------------
   if (tid < NM) {
     uint32_t f = 0;
-    for (int m = 0; m < MP; m++) f = max(f, exp_field(bal[m * NM + tid]));
+    for (int m = 0; m < M; m++) f = max(f, exp_field(alpha_b(p, m, tid)));
     fcol[tid] = (int)f;
   }
   __syncthreads();
-  for (int u = tid; u < NM * (MP / 8); u += THREADS) {  // unit: (n, m-octet)
+  for (int u = tid; u < NM * (MP / 8); u += THREADS) {
     const int n = u % NM, mo = u / NM;
     float d[8][DIGITS];
     bool ng[8];
 #pragma unroll
-    for (int q2 = 0; q2 < 8; q2++) digits_of(bal[(mo * 8 + q2) * NM + n], (uint32_t)fcol[n], d[q2], ng[q2]);
+    for (int q2 = 0; q2 < 8; q2++) digits_of(alpha_b(p, mo * 8 + q2, n), (uint32_t)fcol[n], d[q2], ng[q2]);
 #pragma unroll
     for (int j = 0; j < DIGITS; j++) {
       uint4 w = make_uint4(pack2(d[0][j], d[1][j], ng[0], ng[1]), pack2(d[2][j], d[3][j], ng[2], ng[3]),
@@ -240,27 +217,21 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
   __syncthreads();
   tc_after();
   const uint32_t tmem = *tslot;
-  if (p.bulk && tid == 0)
-    for (int i = 0; i < nt && i < p.stages; i++)
-      if (is_bulk(t_begin + i)) issue(t_begin + i, i);
 
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NM >> 3) << 17) | ((128u >> 4) << 24);
-  const int row = tid & (ROWS - 1), half = tid >> 7;  // slicing: 2 threads per row
+  const int row = tid & (ROWS - 1), half = tid >> 7;
+  const int m0 = half * HALF;
   int uses[2] = {0, 0};
   bool bail = false;
 
-  // epilogue of local tile `it` (TMEM buffer it & 1)
   auto epilogue = [&](int it) {
     const int64_t t = t_begin + it;
     const int64_t r0 = t * ROWS;
     const int rows = (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS);
-    const int b = it & 1;
     const int q = warp & 3;
     const int r = 32 * q + lane;
-    const int* er = erow + (b * 2) * ROWS;  // both halves hold the row maximum
-    const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 8 * NM);
-    const double* T = tile(it % p.stages);
-    // n range of this warp: warps 0-3 take the low half of the columns, 4-7 the high half
+    const int* er = erow + ((it & 1) * 2) * ROWS;
+    const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((it % p.ntbuf) * 8 * NM);
     const int nh = min(N, (((N + 1) / 2) + 1) & ~1);  // even split keeps complex (re, im) pairs together
     const int n0 = (warp < 4) ? 0 : nh, n1 = (warp < 4) ? nh : N;
     for (int c0 = (n0 & ~7); c0 < n1; c0 += 8) {
@@ -271,12 +242,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
       if (r < rows) {
         const int e = er[r];
         double* crow = p.C + (r0 + r) * p.ldc;
-        // old C values of the chunk are read before any of them is overwritten
+        // old C values of the chunk (in place: this row of A, not yet overwritten) before any write
         double cold[8];
 #pragma unroll
         for (int x = 0; x < 8; x++) {
           const int n = c0 + x;
-          cold[x] = (!p.beta_zero && n >= n0 && n < n1) ? (p.inplace ? T[r * p.lda_s + n] : crow[n]) : 0.0;
+          cold[x] = (!p.beta_zero && n >= n0 && n < n1) ? crow[n] : 0.0;
         }
         double out[8];
 #pragma unroll
@@ -284,19 +255,23 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
           const int n = c0 + x;
           out[x] = 0.0;
           if (n < n0 || n >= n1) continue;
-          long long dl[8];
+          // level sums as integers (float-to-int by a magic add where |D_L| <= 2^22)
+          int dl[8];
 #pragma unroll
-          for (int L = 0; L < 8; L++)
-            dl[L] = (long long)(__float_as_int(__uint_as_float(raw[L][x]) + 12582912.0f) - 0x4B400000);
-          const long long H = (dl[0] << 24) + (dl[1] << 16) + (dl[2] << 8) + dl[3];  // levels 2..5
-          const long long Lo = (dl[4] << 24) + (dl[5] << 16) + (dl[6] << 8) + dl[7]; // levels 6..9
-          // V = H * 2^32 + Lo as 128 bits
-          const long long Hh = H >> 32;
-          const unsigned long long Hl = (unsigned long long)H & 0xFFFFFFFFull;
-          const unsigned long long lo0 = Hl << 32;
-          const unsigned long long lo1 = lo0 + (unsigned long long)Lo;
-          const long long hi1 = Hh + (lo1 < lo0 ? 1 : 0) + (Lo < 0 ? -1 : 0);
-          double v = i128_to_double(hi1, lo1, e + fcol[n] - 2112);
+          for (int L = 0; L < 8; L++) {
+            const float f = __uint_as_float(raw[L][x]);
+            dl[L] = MP <= 32 ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
+          }
+          // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
+          const long long H = ((long long)dl[0] * 256 + dl[1]) * 65536 + ((long long)dl[2] * 256 + dl[3]);
+          const long long Lo = ((long long)dl[4] * 256 + dl[5]) * 65536 + ((long long)dl[6] * 256 + dl[7]);
+          // the top 64 bits of V starting at its own leading bit: shift H up by k = clz(|H|) - 1
+          // (k = 32: V fits in 64 bits and is kept whole); the bits of Lo dropped lie below 2^-62
+          // of |V|
+          const long long aH = H < 0 ? -H : H;
+          const int k = aH ? min(32, __clzll(aH) - 1) : 32;
+          const long long top = (H << k) + (Lo >> (32 - k));
+          double v = i64_to_double(top, e + fcol[n] - 2112 + 32 - k);
           if (!p.beta_zero) {
             if (!p.cplx) {
               v = fma(p.beta[0], cold[x], v);
@@ -315,68 +290,56 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
       }
     }
   };
+  auto wait_mma = [&](int tile_it) -> bool {  // wait until the MMAs of local tile tile_it completed
+    const int b = tile_it & 1;
+    return mbar_wait_bounded(&bar_mma[b], (uint32_t)((uses[b] - 1) & 1), p.err);
+  };
 
+  double v[HALF], vn[HALF];
+  if (nt > 0) {
+    const int64_t r0 = t_begin * ROWS;
+    load_row<HALF>(p, r0, row, (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS), m0, v);
+  }
   for (int it = 0; it < nt && !bail; it++) {
     const int64_t t = t_begin + it;
-    const int s = it % p.stages;
     const int64_t r0 = t * ROWS;
-    const int rows = (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS);
-    double* T = tile(s);
-    if (is_bulk(t)) {
-      bool ok = mbar_wait_bounded(&bar_tma[s], (uint32_t)((it / p.stages) & 1), p.err);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
-        break;
-      }
-    } else {
-      const int W = p.wload;
-      for (int e = tid; e < rows * W; e += THREADS) {
-        const int rr = e / W, c = e - rr * W;
-        T[rr * p.lda_s + c] = p.A[(r0 + rr) * p.lda + c];
-      }
-      __syncthreads();
+    if (it + 1 < nt) {  // prefetch the next tile's values into registers
+      const int64_t r1 = r0 + ROWS;
+      load_row<HALF>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, vn);
     }
-    // row exponents (two threads per row: each half of the columns)
-    const int mh = MP / 2, mlo = half * mh;
+    // row exponents: each half of the columns, combined through shared memory
     uint32_t emax = 0;
-    if (row < rows)
-      for (int m = mlo; m < mlo + mh && m < M; m++) emax = max(emax, exp_field(T[row * p.lda_s + m]));
+#pragma unroll
+    for (int j = 0; j < HALF; j++) emax = max(emax, exp_field(v[j]));
     int* er = erow + ((it & 1) * 2) * ROWS;
     er[half * ROWS + row] = (int)emax;
-    // A' buffer free? (the MMAs of tile it - nabuf have completed)
-    const int ab = it % p.nabuf;
     __syncthreads();
     const int e_row = max(er[row], er[ROWS + row]);
-    if (p.nabuf == 1 && it > 0) {
-      const int bp = (it - 1) & 1;
-      bool ok = mbar_wait_bounded(&bar_mma[bp], (uint32_t)((uses[bp] - 1) & 1), p.err);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
-        break;
-      }
-    } else if (p.nabuf == 2 && it > 1) {
-      const int bp = it & 1;  // tile it-2 used TMEM/bar parity it & 1 as well
-      bool ok = mbar_wait_bounded(&bar_mma[bp], (uint32_t)((uses[bp] - 1) & 1), p.err);
+    // the A' buffer is free once the MMAs that read it completed
+    if ((p.nabuf == 1 && it > 0) || (p.nabuf == 2 && it > 1)) {
+      bool ok = wait_mma(it - p.nabuf);
       if (__syncthreads_or(!ok)) {
         bail = true;
         break;
       }
     }
-    // slice: thread (row, half) writes, for each octet of its half of the columns, the 8 digit
-    // planes p = 0..7 (digit 8 - p) at k = p * MP + m
-    unsigned char* A_ = adig + (size_t)ab * p.abuf;
-    for (int mo = mlo / 8; mo < (mlo + mh) / 8; mo++) {
+    unsigned char* A_ = adig + (size_t)(it % p.nabuf) * p.abuf;
+#pragma unroll
+    for (int o = 0; o < HALF / 8; o++) {
+      const int mo = (m0 >> 3) + o;
+      if (mo * 8 >= M) {  // zero padding columns: zero digits
+#pragma unroll
+        for (int pl = 0; pl < DIGITS; pl++)
+          *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) = make_uint4(0, 0, 0, 0);
+        continue;
+      }
       float d[8][DIGITS];
       bool ng[8];
 #pragma unroll
-      for (int q2 = 0; q2 < 8; q2++) {
-        const int m = mo * 8 + q2;
-        const double x = (row < rows && m < M) ? T[row * p.lda_s + m] : 0.0;
-        digits_of(x, (uint32_t)e_row, d[q2], ng[q2]);
-      }
+      for (int q2 = 0; q2 < 8; q2++) digits_of(v[o * 8 + q2], (uint32_t)e_row, d[q2], ng[q2]);
 #pragma unroll
       for (int pl = 0; pl < DIGITS; pl++) {
-        const int i = 7 - pl;  // digit index (0-based) stored in plane pl
+        const int i = 7 - pl;  // 0-based digit index held by plane pl
         uint4 w = make_uint4(pack2(d[0][i], d[1][i], ng[0], ng[1]), pack2(d[2][i], d[3][i], ng[2], ng[3]),
                              pack2(d[4][i], d[5][i], ng[4], ng[5]), pack2(d[6][i], d[7][i], ng[6], ng[7]));
         *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) = w;
@@ -386,25 +349,35 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     fence_proxy_async_smem();
     tc_before();
     __syncthreads();
+    if (p.ntbuf == 1 && it > 0) {  // one accumulator: drain tile it-1 before tile it's MMAs
+      if (p.nabuf != 1) {
+        bool ok = wait_mma(it - 1);
+        if (__syncthreads_or(!ok)) {
+          bail = true;
+          break;
+        }
+      }
+      tc_after();
+      epilogue(it - 1);
+      tc_before();
+      __syncthreads();
+    }
     if (tid == 0) {
       tc_after();
-      const int b = it & 1;
       const uint32_t a0 = smem_u32(A_), b0 = smem_u32(bdig);
-      const uint32_t dcol = tmem + (uint32_t)(b * 8 * NM);
+      const uint32_t dcol = tmem + (uint32_t)((it % p.ntbuf) * 8 * NM);
       for (int L = 2; L <= 9; L++) {
-        const int kq = (L - 1) * MP / 16;    // K-steps of 16
-        const int ka = (9 - L) * MP / 8;     // first k-octet of A' for this level
+        const int kq = (L - 1) * MP / 16;  // K-steps of 16
+        const int ka = (9 - L) * MP / 8;   // first k-octet of A' for this level
         for (int ks = 0; ks < kq; ks++)
           mma_bf16(dcol + (uint32_t)((L - 2) * NM), make_desc(a0 + (uint32_t)(ka + 2 * ks) * lbo_a, lbo_a),
                    make_desc(b0 + (uint32_t)(2 * ks) * lbo_b, lbo_b), idesc, ks > 0 ? 1u : 0u);
       }
-      mma_commit(&bar_mma[b]);
+      mma_commit(&bar_mma[it & 1]);
     }
     uses[it & 1]++;
-    // epilogue of the previous tile overlaps this tile's MMAs
-    if (it > 0) {
-      const int bp = (it - 1) & 1;
-      bool ok = mbar_wait_bounded(&bar_mma[bp], (uint32_t)((uses[bp] - 1) & 1), p.err);
+    if (p.ntbuf == 2 && it > 0) {  // the previous tile's epilogue overlaps this tile's MMAs
+      bool ok = wait_mma(it - 1);
       if (__syncthreads_or(!ok)) {
         bail = true;
         break;
@@ -413,20 +386,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
       epilogue(it - 1);
       tc_before();
       __syncthreads();
-      // FP64 stage of tile it-1 is free now (its epilogue may have read it in place)
-      if (tid == 0 && p.bulk) {
-        const int sp = (it - 1) % p.stages;
-        const int64_t tn = t - 1 + p.stages;
-        if (it - 1 + p.stages < nt && is_bulk(tn)) {
-          fence_proxy_async_smem();
-          issue(tn, sp);
-        }
-      }
     }
+#pragma unroll
+    for (int j = 0; j < HALF; j++) v[j] = vn[j];
   }
   if (!bail && nt > 0) {
-    const int bl = (nt - 1) & 1;
-    bool ok = mbar_wait_bounded(&bar_mma[bl], (uint32_t)((uses[bl] - 1) & 1), p.err);
+    bool ok = wait_mma(nt - 1);
     if (__syncthreads_or(!ok)) {
       bail = true;
     } else {
@@ -449,13 +414,15 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
                          int64_t ldc, cudaStream_t st, bool autoselect) {
   using namespace stsmm;
   const int64_t Mr = cplx ? 2 * M : M, Nr = cplx ? 2 * N : N;
-  if (Mr > 32 || Nr > 32) {
-    set_error("split precision TSMM: real widths M, N <= 32 in this build");
+  if (Mr > 64 || Nr > 64) {
+    set_error("split precision TSMM: real widths M, N <= 64 in this build");
     return SKINNY_UNSUPPORTED;
   }
-  // auto selection (measured on GB300): split wins from real widths Mr * Nr >= 512 on (FP64 32x32,
-  // complex 16x16); below that the CUDA-core kernels are as fast.  The autotuner can override.
-  if (autoselect && (K < 8192 || Mr * Nr < 512)) {
+  // auto selection (measured on GB300, K with A of 1 GiB): FP64 split wins when both widths are
+  // >= 16 (1.07x at 16x16 .. 5x at 64x64); complex FP64 from M*N >= 64 (1.16x at 4x16, 5.2x at
+  // 32x32).  Below that the CUDA-core kernels are faster.  The autotuner can override.
+  const bool wins = cplx ? (M * N >= 64) : (Mr >= 16 && Nr >= 16);
+  if (autoselect && (K < 8192 || !wins)) {
     set_error("split precision TSMM: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
   }
@@ -469,8 +436,8 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   a.ldc = cplx ? 2 * ldc : ldc;
   a.M = (int)Mr;
   a.N = (int)Nr;
-  a.MP = Mr <= 16 ? 16 : 32;
-  a.NM = Nr <= 16 ? 16 : 32;
+  const int MP = Mr <= 16 ? 16 : (Mr <= 32 ? 32 : 64);
+  a.NM = Nr <= 16 ? 16 : (Nr <= 32 ? 32 : 64);
   a.cplx = cplx;
   std::memset(a.alpha, 0, sizeof a.alpha);
   std::memset(a.beta, 0, sizeof a.beta);
@@ -478,37 +445,45 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   std::memcpy(a.beta, beta, cplx ? 16 : 8);
   a.beta_zero = a.beta[0] == 0.0 && a.beta[1] == 0.0;
   a.inplace = (const void*)A == (const void*)C;
-  const bool aligned = (uintptr_t)A % 16 == 0;
-  const bool dense = a.lda <= 2 * Mr + 16;
-  a.bulk = aligned && dense && K > ROWS;
-  a.wload = (int)(a.inplace ? std::max(Mr, Nr) : Mr);
-  a.lda_s = a.bulk ? a.lda : a.wload;
-  a.tile_bytes = (uint32_t)round_up(ROWS * a.lda_s * 8, 1024);
-  a.abuf = (uint32_t)(ROWS * 8 * a.MP * 2);  // 128 rows x 8 planes x MP x bf16
-  const uint32_t bdig = (uint32_t)round_up((int64_t)8 * a.MP * a.NM * 2, 1024);
-  const int64_t fixed = HDR + BAL + bdig;
-  a.nabuf = 2;
-  int stages = (int)std::min<int64_t>(4, (h->dev.smem_optin - fixed - 2 * (int64_t)a.abuf) / a.tile_bytes);
-  if (stages < 3) {
-    a.nabuf = 1;
-    stages = (int)std::min<int64_t>(4, (h->dev.smem_optin - fixed - (int64_t)a.abuf) / a.tile_bytes);
-  }
-  if (stages < 2 || (a.inplace && stages < 3)) {
+  a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
+  a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x bf16
+  const int64_t bdig = round_up((int64_t)8 * MP * a.NM * 2, 1024);
+  const int64_t avail = h->dev.smem_optin - HDR - bdig;
+  a.nabuf = avail >= 2 * (int64_t)a.abuf ? 2 : 1;
+  if (avail < (int64_t)a.abuf) {
     set_error("split precision TSMM: tiles do not fit in shared memory");
     return SKINNY_UNSUPPORTED;
   }
-  a.stages = stages;
+  a.ntbuf = 2 * 8 * a.NM <= 512 ? 2 : 1;
+  a.tmem_cols = a.ntbuf * 8 * a.NM <= 256 ? 256 : 512;
   a.ntiles = (K + ROWS - 1) / ROWS;
-  a.tmem_cols = 2 * 8 * a.NM <= 256 ? 256 : 512;
   a.err = h->err;
-  const int smem = (int)(fixed + (int64_t)a.nabuf * a.abuf + (int64_t)stages * a.tile_bytes);
+  const int smem = (int)(HDR + bdig + (int64_t)a.nabuf * a.abuf);
   int64_t grid = std::min<int64_t>(h->dev.sms, a.ntiles);
   if (grid < 1) grid = 1;
-  static std::atomic<int> attr{0};
-  ensure_smem_attr(split_tsmm_kernel, smem, attr);
-  split_tsmm_kernel<<<(int)grid, THREADS, smem, st>>>(a);
+  cudaError_t e;
+  switch (MP) {
+    case 16: {
+      static std::atomic<int> attr{0};
+      ensure_smem_attr(split_tsmm_kernel<16>, smem, attr);
+      split_tsmm_kernel<16><<<(int)grid, THREADS, smem, st>>>(a);
+      break;
+    }
+    case 32: {
+      static std::atomic<int> attr{0};
+      ensure_smem_attr(split_tsmm_kernel<32>, smem, attr);
+      split_tsmm_kernel<32><<<(int)grid, THREADS, smem, st>>>(a);
+      break;
+    }
+    default: {
+      static std::atomic<int> attr{0};
+      ensure_smem_attr(split_tsmm_kernel<64>, smem, attr);
+      split_tsmm_kernel<64><<<(int)grid, THREADS, smem, st>>>(a);
+      break;
+    }
+  }
   count_launch();
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("split tsmm launch: ") + cudaGetErrorString(e));
     return SKINNY_DEVICE_ERROR;
