@@ -22,7 +22,8 @@ def host(t):
     return t.cpu().numpy()
 
 
-SPLIT_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and not c["cplx"] and c["M"] <= 16 and c["N"] <= 16]
+SPLIT_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and not c["cplx"] and c["M"] <= 128 and
+               c["N"] <= 128]
 
 
 @pytest.mark.parametrize("case", SPLIT_CASES, ids=lambda c: c["id"])
@@ -107,7 +108,7 @@ def test_split_unaligned_padded_and_zero_columns(handle):
 
 def test_split_deterministic_and_auto(handle):
     rng = np.random.default_rng(2)
-    M = N = 8
+    M = N = 16  # auto picks the split kernel from M * N >= 256 on
     K = 1 << 20
     A, B = dev(rng.uniform(-1, 1, K * M)), dev(rng.uniform(-1, 1, K * N))
     outs = []
@@ -117,3 +118,72 @@ def test_split_deterministic_and_auto(handle):
         outs.append(host(Cd))
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
     handle.check_device()
+
+
+# M or N > 16: the product is formed as 16 x 16 blocks of C in one launch; Gram computes the upper
+# blocks only and mirrors them
+BLOCKED = [(32, 32, 20011), (64, 64, 8192), (128, 128, 4099), (17, 40, 7000), (64, 20, 9000), (20, 64, 9000),
+           (128, 16, 3000), (1, 128, 3000), (33, 33, 129)]
+
+
+@pytest.mark.parametrize("M,N,K", BLOCKED)
+def test_split_blocked_vs_exact(handle, M, N, K):
+    rng = np.random.default_rng(M * 131 + N * 7 + K)
+    lda, ldb, ldc = M + 1, N, M + 3
+    A = rng.uniform(-1, 1, K * lda)
+    B = rng.uniform(-1, 1, K * ldb)
+    C0 = rng.uniform(-1, 1, N * ldc)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), lda, 0.75, dev(B), ldb, 1.5, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, N, K, A, lda, B, ldb, C0, ldc, 0.75, 1.5)
+    err = common.normwise(got, exp, den, common.c_mask_tsmttsm(M, N, ldc))
+    assert err <= 4e-16, err
+    assert np.array_equal(got[~common.c_mask_tsmttsm(M, N, ldc)], C0[~common.c_mask_tsmttsm(M, N, ldc)])
+
+
+@pytest.mark.parametrize("M", [17, 32, 40, 64, 128])
+@pytest.mark.parametrize("beta", [0.0, -0.5])
+def test_split_blocked_gram_mirrored(handle, M, beta):
+    rng = np.random.default_rng(M + 7)
+    K = 6000 if M == 128 else 30000
+    X = common.spread(rng, K * M)
+    C0 = rng.uniform(-1, 1, M * M)
+    Cd = dev(C0)
+    Xd = dev(X)
+    handle.tsmttsm(M, M, K, Xd, M, 1.0, Xd, M, beta, Cd, M, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, M, K, X, M, X, M, C0, M, 1.0, beta)
+    assert common.normwise(got, exp, den) <= 1e-15
+    if beta == 0.0:
+        G = got.reshape(M, M)
+        assert np.array_equal(G, G.T)
+
+
+def test_split_blocked_wide_exponents_and_determinism(handle):
+    rng = np.random.default_rng(9)
+    M = N = 64
+    K = 1 << 16
+    A, B = common.spread(rng, K * M), common.spread(rng, K * N)
+    Ad, Bd = dev(A), dev(B)
+    outs = []
+    for _ in range(2):
+        Cd = dev(np.zeros(M * N))
+        handle.tsmttsm(M, N, K, Ad, M, 1.0, Bd, N, 0.0, Cd, M, acc="split")
+        outs.append(host(Cd))
+    assert np.array_equal(outs[0], outs[1])
+    exp, den = common.tsmttsm_expected(M, N, K, A, M, B, N, np.zeros(M * N), M, 1.0, 0.0)
+    assert common.normwise(outs[0], exp, den) <= 1e-15
+
+
+def test_split_beyond_128_unsupported_and_auto_falls_back(handle):
+    from skinny_matmul_gb300 import lib as L
+    M, N, K = 136, 8, 4096
+    rng = np.random.default_rng(1)
+    A, B = dev(rng.uniform(-1, 1, K * M)), dev(rng.uniform(-1, 1, K * N))
+    Cd = dev(np.zeros(M * N))
+    with pytest.raises(L.SkinnyError):
+        handle.tsmttsm(M, N, K, A, M, 1.0, B, N, 0.0, Cd, M, acc="split")
+    handle.tsmttsm(M, N, K, A, M, 1.0, B, N, 0.0, Cd, M, acc="auto")  # native FP64
+    exp, den = common.tsmttsm_expected(M, N, K, host(A), M, host(B), N, np.zeros(M * N), M, 1.0, 0.0)
+    assert common.normwise(host(Cd), exp, den) <= common.tol(np.float64, K)
