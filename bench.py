@@ -150,9 +150,18 @@ def probe_split_items():
     return probe_tsmttsm_items()
 
 
+def probe_split_wide_items():
+    M = N = 64
+    K = 1 << 21
+    return [dict(op="tsmttsm", dt="f64", M=M, N=N, K=K, inplace=False, s=8, bytes=(M + N) * K * 8,
+                 flops=2 * M * N * K, copies=1)]
+
+
 WORKLOADS = {
     "probe-split-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-split": (probe_split_items, "TSMTTSM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
+    "probe-split-wide": (probe_split_wide_items, "TSMTTSM FP64 64x64, K = 2^21 (2 x 1 GiB), run with --method "
+                         "split: small case for ncu"),
     "probe-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22 (256 MiB A), alpha 1, beta 0.5: small case for ncu"),
     "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),
     "tsmm-sweep": (sweep_items, "TSMM FP64 + complex FP64, alpha 1, beta 0.5, A = 1 GiB per shape, "

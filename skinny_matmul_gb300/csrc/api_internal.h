@@ -66,6 +66,11 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
                             int64_t ldb, const void* beta, double* C, int64_t ldc,
                             cudaStream_t st, bool autoselect);
 
+// FP64 TSMTTSM in split precision for M or N in 17..128 (split_wide.cu); SKINNY_UNSUPPORTED beyond.
+skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
+                         const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
+                         int64_t ldc, cudaStream_t st);
+
 // FP64 / complex FP64 TSMM in split precision (split_tsmm.cu); SKINNY_UNSUPPORTED outside its range.
 skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64_t K, const double* A,
                          int64_t lda, const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,

@@ -1,5 +1,6 @@
-// split.cu -- FP64 TSMTTSM in split precision on tcgen05 tensor cores (no counterpart in the
-// reference, whose FP64 kernels are CUDA-core DFMA loops, e.g. tsmttsm/genv5.cuh:28-89).
+// split.cu -- FP64 TSMTTSM in split precision on tcgen05 tensor cores for M, N <= 16 (no
+// counterpart in the reference, whose FP64 kernels are CUDA-core DFMA loops, e.g.
+// tsmttsm/genv5.cuh:28-89).  Wider products go to split_wide.cu.
 //
 // Why: GB300 executes 595 G FP64 FMA/s but 2.25 P BF16 tensor flop/s.  A CUDA-core FP64 TSMTTSM
 // is FP64-bound for every M = N >= 2.  Here each FP64 product is computed exactly from 8-bit
@@ -65,24 +66,7 @@ struct Args {
   double* partials;
   unsigned* counter;
   int* err;
-  // 16 x 16 blocks of C for M or N > 16: block b of nblk covers columns [16 bi, 16 bi + 16) of A
-  // and [16 bj, 16 bj + 16) of B; sym: Gram, only bi <= bj computed, the mirror written too
-  int nblk, bm, bn, sym;
 };
-
-__device__ __forceinline__ void block_coords(int b, int bm, int bn, int sym, int& bi, int& bj) {
-  if (!sym) {
-    bi = b % bm;
-    bj = b / bm;
-    return;
-  }
-  bj = 0;  // upper triangle, column by column: (0,0), (0,1), (1,1), (0,2), ...
-  while (b > bj) {
-    b -= bj + 1;
-    bj++;
-  }
-  bi = b;
-}
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo) {
   uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
@@ -187,23 +171,8 @@ __device__ __forceinline__ void slice_unit(const double (&v)[8], uint32_t E, int
 }
 
 template <int NP>
-__global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p0) {
-  // this CTA's block of C and its chunk of the K rows (blocks vary fastest across CTAs so that the
-  // CTAs reading the same rows run together and share them through L2)
-  const int blk = blockIdx.x % p0.nblk, chunk = blockIdx.x / p0.nblk, nchunks = gridDim.x / p0.nblk;
-  int bi = 0, bj = 0;
-  block_coords(blk, p0.bm, p0.bn, p0.sym, bi, bj);
-  Args p = p0;
-  if (p0.nblk > 1) {
-    p.M = min(16, p0.M - 16 * bi);
-    p.N = min(16, p0.N - 16 * bj);
-    p.A = p0.A + 16 * bi;
-    p.B = (p0.sym ? p0.A : p0.B) + 16 * bj;
-    p.gram = p0.sym && bi == bj;
-    p.C = p0.C + (int64_t)(16 * bj) * p0.ldc + 16 * bi;
-    p.partials = p0.partials + (size_t)blk * nchunks * 256;
-    p.counter = p0.counter + blk;
-  }
+__global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p) {
+  const int chunk = blockIdx.x, nchunks = gridDim.x;
   constexpr int BN = NP < 8 ? NP : 8;  // n per drain block
   constexpr int NB = NP / BN;          // drain blocks
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -503,10 +472,6 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p0
     const int mm = tid % M, nn = tid / M;
     double* c = p.C + (int64_t)nn * p.ldc + mm;
     *c = p.beta_zero ? p.alpha * sum : (*c) * p.beta + sum * p.alpha;
-    if (p0.sym && bi < bj) {  // Gram: the mirrored block holds the same sums
-      double* cm = p0.C + (int64_t)(16 * bi + mm) * p0.ldc + 16 * bj + nn;
-      *cm = p.beta_zero ? p.alpha * sum : (*cm) * p.beta + sum * p.alpha;
-    }
   }
   if (tid == 0) *p.counter = 0u;
 }
@@ -534,22 +499,25 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
                             cudaStream_t st, bool autoselect) {
   using namespace split;
   if (tsmm) return split_tsmm(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, autoselect);
-  // M or N > 16: 16 x 16 blocks of C in one launch (at most 64 blocks: one ticket counter each)
-  const bool blocked = M > 16 || N > 16;
-  const int bm = (int)((M + 15) / 16), bn = (int)((N + 15) / 16);
-  const bool sym_all = (A == B) && (lda == ldb) && (M == N);
-  const int nblk = !blocked ? 1 : (sym_all ? bm * (bm + 1) / 2 : bm * bn);
   if (M > 128 || N > 128) {
-    set_error("split precision TSMTTSM: M, N <= 128 (64 blocks of 16 x 16)");
+    set_error("split precision TSMTTSM: M, N <= 128");
     return SKINNY_UNSUPPORTED;
   }
   // auto selection (measured on GB300): the split kernel wins from M*N >= 256 on; below that the
-  // CUDA-core FP64 kernel is as fast or faster.  The autotuner can override per shape.
-  // 16 x 16 blocks slice every column once per block; measured, only Gram from M = 64 on gains
-  if (autoselect && (K < 4096 || M * N < 256 || (blocked && !(sym_all && M >= 64)))) {
+  // CUDA-core FP64 kernel is as fast or faster.  The wide kernel costs about as much per 64 x 64
+  // block whatever the block's fill (12.5 ms per block at K = 2^24; CUDA-core FP64 takes 23 ms at
+  // M = N = 17 and 114 ms at 64), so it is chosen from M*N >= 320 per block on.  The autotuner can
+  // override per shape.
+  const bool wide = M > 16 || N > 16;
+  const int64_t sym_w = (A == B && lda == ldb && M == N) ? 1 : 0;
+  const int64_t bm = (M + 63) / 64, bn = (N + 63) / 64;
+  const int64_t nblk_w = sym_w ? bm * (bm + 1) / 2 : bm * bn;
+  if (autoselect && (K < 4096 || M * N < 256 || (wide && M * N < 320 * nblk_w))) {
     set_error("split precision: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
   }
+  // M or N > 16: the wide kernel (64 x 64 blocks, FP16 digit planes, level accumulators)
+  if (wide) return split_wide(h, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st);
   Args a;
   a.A = A;
   a.B = B;
@@ -563,13 +531,9 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   std::memcpy(&a.alpha, alpha, 8);
   std::memcpy(&a.beta, beta, 8);
   a.beta_zero = a.beta == 0.0;
-  a.gram = !blocked && sym_all;
-  const int NP = blocked ? 16 : pow2ceil(a.gram ? M : N);
-  a.MP = blocked ? 16 : (a.gram ? NP : pow2ceil(M));
-  a.nblk = nblk;
-  a.bm = bm;
-  a.bn = bn;
-  a.sym = blocked && sym_all;
+  a.gram = (A == B) && (lda == ldb) && (M == N);
+  const int NP = pow2ceil(a.gram ? M : N);
+  a.MP = a.gram ? NP : pow2ceil(M);
   // windows per iteration: the largest power of two (<= PERIOD / W) whose slicing units
   // (k-octet x column; A units padded to a warp multiple) fit two per thread
   auto units = [&](int w) {
@@ -585,11 +549,11 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   const int64_t RSW = (int64_t)sw * W;
   const bool aligned = ((uintptr_t)A % 16 == 0) && (a.gram || (uintptr_t)B % 16 == 0);
   const bool dense = lda <= 2 * M + 16 && (a.gram || ldb <= 2 * N + 16);
-  a.bulk = aligned && dense && K > RSW && !blocked;  // blocks load their 16 columns with plain loads
-  a.lda_s = a.bulk ? lda : (blocked ? 16 : M);
-  a.ldb_s = a.gram ? a.lda_s : (a.bulk ? ldb : (blocked ? 16 : N));
+  a.bulk = aligned && dense && K > RSW;
+  a.lda_s = a.bulk ? lda : M;
+  a.ldb_s = a.gram ? a.lda_s : (a.bulk ? ldb : N);
   a.tile_a = (uint32_t)round_up(RSW * a.lda_s * 8, 128);
-  a.tile_b = (a.gram && !blocked) ? 0u : (uint32_t)round_up(RSW * a.ldb_s * 8, 128);
+  a.tile_b = a.gram ? 0u : (uint32_t)round_up(RSW * a.ldb_s * 8, 128);
   a.nmma = std::max(16, 8 * NP);
   a.tmem_cols = a.nmma <= 32 ? 32 : (a.nmma <= 64 ? 64 : 128);
   a.lbo_a = (uint32_t)(8 * a.MP * 16);
@@ -612,10 +576,9 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.stages = stages;
   a.ntiles = (K + RSW - 1) / RSW;
   const int smem2 = (int)(fixed + stages * stage);
-  int64_t nchunks = std::max<int64_t>(1, std::min<int64_t>(a.ntiles, h->dev.sms / nblk));
-  const int64_t grid = nchunks * nblk;
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(a.ntiles, h->dev.sms));
   Workspace& ws = h->ws[st];
-  skinny_status s = workspace_ensure(ws, blocked ? (size_t)grid * 256 * 8 : (size_t)grid * M * N * 8, st);
+  skinny_status s = workspace_ensure(ws, (size_t)grid * M * N * 8, st);
   if (s != SKINNY_OK) return s;
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;

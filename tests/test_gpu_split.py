@@ -120,16 +120,19 @@ def test_split_deterministic_and_auto(handle):
     handle.check_device()
 
 
-# M or N > 16: the product is formed as 16 x 16 blocks of C in one launch; Gram computes the upper
-# blocks only and mirrors them
+# M or N > 16: the wide kernel (64 x 64 blocks of C in one launch, each element sliced once per
+# block row / column; Gram computes the upper blocks only and mirrors them)
 BLOCKED = [(32, 32, 20011), (64, 64, 8192), (128, 128, 4099), (17, 40, 7000), (64, 20, 9000), (20, 64, 9000),
-           (128, 16, 3000), (1, 128, 3000), (33, 33, 129)]
+           (128, 16, 3000), (1, 128, 3000), (33, 33, 129), (65, 63, 5000), (96, 128, 2000), (128, 1, 999)]
 
 
 @pytest.mark.parametrize("M,N,K", BLOCKED)
-def test_split_blocked_vs_exact(handle, M, N, K):
-    rng = np.random.default_rng(M * 131 + N * 7 + K)
-    lda, ldb, ldc = M + 1, N, M + 3
+@pytest.mark.parametrize("pad", [0, 1, 2])
+def test_split_blocked_vs_exact(handle, M, N, K, pad):
+    """pad 0: dense rows (whole stages by one copy); 1: odd leading dimension (8-byte copies);
+    2: even padded rows (one bulk copy per row)."""
+    rng = np.random.default_rng(M * 131 + N * 7 + K + pad)
+    lda, ldb, ldc = M + pad, N + pad, M + 3
     A = rng.uniform(-1, 1, K * lda)
     B = rng.uniform(-1, 1, K * ldb)
     C0 = rng.uniform(-1, 1, N * ldc)
@@ -187,3 +190,49 @@ def test_split_beyond_128_unsupported_and_auto_falls_back(handle):
     handle.tsmttsm(M, N, K, A, M, 1.0, B, N, 0.0, Cd, M, acc="auto")  # native FP64
     exp, den = common.tsmttsm_expected(M, N, K, host(A), M, host(B), N, np.zeros(M * N), M, 1.0, 0.0)
     assert common.normwise(host(Cd), exp, den) <= common.tol(np.float64, K)
+
+
+def test_split_wide_growing_exponents_and_zero_columns(handle):
+    """Column maxima rise along K (new exponent epochs mid-stream), some columns are zero, others
+    are zero until late."""
+    rng = np.random.default_rng(21)
+    M, N, K = 64, 48, 150001
+    scale = np.ldexp(1.0, (np.arange(K) // 7000) - 10)
+    A = (rng.uniform(-1, 1, (K, M)) * scale[:, None])
+    B = rng.uniform(-1, 1, (K, N))
+    A[:, 5] = 0.0
+    B[:, 7] = 0.0
+    A[: K // 2, 9] = 0.0
+    B[: K - 100, 11] = 0.0
+    A, B = A.ravel(), B.ravel()
+    Cd = dev(np.zeros(M * N))
+    handle.tsmttsm(M, N, K, dev(A), M, 1.0, dev(B), N, 0.0, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, N, K, A, M, B, N, np.zeros(M * N), M, 1.0, 0.0)
+    assert common.normwise(host(Cd), exp, den) <= 4e-16
+
+
+@pytest.mark.parametrize("M,N,lda,ldb,off", [(33, 31, 33, 31, 0), (40, 40, 41, 43, 0), (64, 64, 64, 64, 1),
+                                              (17, 64, 20, 70, 1)])
+def test_split_wide_unaligned_and_odd(handle, M, N, lda, ldb, off):
+    rng = np.random.default_rng(M + N + lda)
+    K = 20000
+    A = rng.uniform(-1, 1, K * lda + 1)
+    B = rng.uniform(-1, 1, K * ldb + 1)
+    Ad, Bd = dev(A), dev(B)
+    Cd = dev(np.zeros(N * M))
+    handle.tsmttsm(M, N, K, Ad[off:], lda, 1.0, Bd[off:], ldb, 0.0, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, N, K, A[off:].copy(), lda, B[off:].copy(), ldb, np.zeros(M * N), M, 1.0,
+                                       0.0)
+    assert common.normwise(host(Cd), exp, den) <= 4e-16
+
+
+@pytest.mark.parametrize("K", [1, 15, 16, 17, 127, 128, 129, 2047, 2048, 2049])
+def test_split_wide_small_k(handle, K):
+    rng = np.random.default_rng(K)
+    M, N = 48, 64
+    A, B = rng.uniform(-1, 1, K * M), rng.uniform(-1, 1, K * N)
+    C0 = rng.uniform(-1, 1, M * N)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), M, 2.0, dev(B), N, 0.5, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, N, K, A, M, B, N, C0, M, 2.0, 0.5)
+    assert common.normwise(host(Cd), exp, den) <= 4e-16
