@@ -130,6 +130,18 @@ def c1_items():
                  flops=2 * M * N * K, copies=16)]
 
 
+def c3_items():
+    K = 1 << 24
+    return [dict(op="tsmttsm", dt="f64", M=M, N=M, K=K, inplace=False, s=8, bytes=2 * M * K * 8,
+                 flops=2 * M * M * K, copies=1) for M in (32, 64, 128)]
+
+
+def c4_items():
+    K = 1 << 24
+    return [dict(op="tsmttsm", dt="f64", M=M, N=M, K=K, inplace=False, s=8, bytes=3 * M * K * 8,
+                 flops=4 * M * M * K, copies=1) for M in (16, 32, 64)]
+
+
 def probe_tsmm_items():
     M = N = 8
     K = 1 << 22
@@ -168,6 +180,10 @@ WORKLOADS = {
                    "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
     "tsmttsm-c1": (c1_items, "TSMTTSM FP64 C(8x8) = A^T B, K = 2^20, alpha 1, beta 0, "
                    "16 rotating input copies (2 GiB > L2)"),
+    "svqb-c4": (c4_items, "SVQB of X (K = 2^24, M in {16, 32, 64}, condition 1e8), Gram in plain FP64, split "
+                "precision or double-double; time and ||Q^T Q - I||_F"),
+    "precision-c3": (c3_items, "TSMTTSM FP64 M = N in {32, 64, 128}, K = 2^24, entries s*2^e, plain FP64 vs "
+                     "split precision vs double-double; normwise error against the double-double result"),
 }
 
 
@@ -326,6 +342,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "precision-c3":
+        return run_precision(args)
+    if args.workload == "svqb-c4":
+        return run_svqb(args)
 
     import torch
     from skinny_matmul_gb300 import Handle, build, lib
@@ -425,6 +445,178 @@ def main():
 
 # DRAM bytes per step of the dominant kernel from one ncu capture (profiles/), or None.
 TRAFFIC = {}
+
+
+# --------------------------------------------------------------------------------- SVQB (C4)
+def svqb_operand(K, M, cond, gen, device):
+    """X = G R: G standard Gaussian K x M, R upper triangular with singular values log-spaced from
+    1 to 1/cond (R is the triangular factor of U diag(sigma) V^T, U and V orthogonal factors of
+    seeded Gaussian matrices)."""
+    import torch
+    U, _ = torch.linalg.qr(torch.randn(M, M, dtype=torch.float64, device=device, generator=gen))
+    V, _ = torch.linalg.qr(torch.randn(M, M, dtype=torch.float64, device=device, generator=gen))
+    sig = torch.logspace(0, -math.log10(cond), M, dtype=torch.float64, device=device)
+    _, R = torch.linalg.qr(U @ torch.diag(sig) @ V.T)
+    G = torch.randn(K, M, dtype=torch.float64, device=device, generator=gen)
+    return (G @ R).contiguous().view(-1)
+
+
+def run_svqb(args):
+    """SVQB of X (K = 2^24, M in {16, 32, 64}, condition 1e8): Gram S = X^T X, diagonal scaling,
+    on-device FP64 eigensolve, X <- X (D^-1/2 U Lambda^-1/2) by in-place TSMM; the Gram in plain
+    FP64, split precision or double-double.  Reports time and ||Q^T Q - I||_F per Gram method."""
+    import torch
+    from skinny_matmul_gb300 import Handle, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    K = 1 << 24
+    rows = []
+    n0 = L.skinny_kernel_launches()
+    total_bytes, total_ms = 0.0, 0.0
+    with ClockSampler(local) as clk:
+        for M in (16, 32, 64):
+            g = torch.Generator(device=dev).manual_seed(777 + M + 13 * rank)
+            X0 = svqb_operand(K, M, 1e8, g, dev)
+            X = torch.empty_like(X0)
+            for meth in ("native", "split", "dd"):
+                ts, errs = [], []
+                for it in range(max(1, args.warmup // 3) + max(1, min(args.steps, 3))):
+                    X.copy_(X0)
+                    torch.cuda.synchronize()
+                    barrier(world)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    h.svqb(K, M, X, M, gram_acc=meth, orth_err=False)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    if it >= max(1, args.warmup // 3):
+                        ts.append(max_over_ranks(e0.elapsed_time(e1), world))
+                X.copy_(X0)
+                err = h.svqb(K, M, X, M, gram_acc=meth, orth_err=True)
+                ms = sorted(ts)[len(ts) // 2]
+                by = 3 * K * M * 8
+                rows.append({"M": M, "K": K, "cond": 1e8, "gram": meth, "ms": round(ms, 3),
+                             "GB/s": round(by / (ms * 1e-3) / 1e9, 1), "orth_err": err})
+                total_bytes += by
+                total_ms += ms
+            del X0, X
+            torch.cuda.empty_cache()
+    launches = L.skinny_kernel_launches() - n0
+    h.check_device()
+    if rank == 0:
+        hbm, _ = peaks()
+        value = total_bytes / (total_ms * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(total_ms, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic X = G R (Gaussian G, triangular R with singular values 1..1e-8), seeded",
+                "config": {"workload": "svqb-c4", "description": WORKLOADS["svqb-c4"][1],
+                           "l2": "operands larger than L2 (no flush needed)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "hbm", "achieved": round(value, 1), "peak": hbm, "unit": "GB/s",
+                             "frac": round(value / hbm, 4), "traffic": None, "kernel": "svqb pipeline",
+                             "note": "3 K M 8 bytes per SVQB (Gram read, TSMM read and write)"},
+                "svqb": rows, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": None,
+                "e2e": None}
+        print(json.dumps(line), flush=True)
+    h.close()
+
+
+# ------------------------------------------------------------------------ precision (TSMTTSM C3)
+def spread_operand(n, gen, device):
+    """Entries s * 2^e: s uniform in [1, 2), random sign, e uniform integer in [-20, 20]."""
+    import torch
+    s = torch.rand(n, dtype=torch.float64, device=device, generator=gen) + 1.0
+    sign = torch.randint(0, 2, (n,), device=device, generator=gen, dtype=torch.int32) * 2 - 1
+    e = torch.randint(-20, 21, (n,), device=device, generator=gen, dtype=torch.int32)
+    return torch.ldexp(s * sign, e)
+
+
+def run_precision(args):
+    """FP64 TSMTTSM C = A^T B at M = N in {32, 64, 128}, K = 2^24, entries s * 2^e, three ways:
+    CUDA-core FP64 ("native"), split precision on the tensor cores ("split") and double-double
+    accumulation ("dd", the reference's PseudoQuad form).  Errors are normwise,
+    ||C - C_dd||_F / || |A|^T |B| ||_F, against the double-double result of the same launch data
+    (the dd method itself is pinned against the exact super-accumulator by the GPU tests)."""
+    import torch
+    from skinny_matmul_gb300 import Handle, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    K = 1 << 24
+    rows = []
+    n0 = L.skinny_kernel_launches()
+    hbm, peak_kind = peaks()
+    total_bytes, total_ms = 0.0, 0.0
+    with ClockSampler(local) as clk:
+        for M in (32, 64, 128):
+            g = torch.Generator(device=dev).manual_seed(4242 + M + 13 * rank)
+            A = spread_operand(K * M, g, dev)
+            B = spread_operand(K * M, g, dev)
+            out = {}
+            for meth in ("dd", "native", "split"):
+                C = torch.zeros(M * M, dtype=torch.float64, device=dev)
+                for _ in range(max(1, args.warmup if meth == "split" else 1)):
+                    h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
+                steps = args.steps if meth == "split" else max(1, min(args.steps, 2))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                barrier(world)
+                torch.cuda.synchronize()
+                e0.record()
+                for _ in range(steps):
+                    h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = max_over_ranks(e0.elapsed_time(e1) / steps, world)
+                out[meth] = (C.clone(), ms)
+                if meth == "split":
+                    total_bytes += 2 * M * K * 8 * steps
+                    total_ms += ms * steps
+            A.abs_()
+            B.abs_()
+            D = torch.zeros(M * M, dtype=torch.float64, device=dev)
+            h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, D, M, acc="native")
+            den = float(torch.linalg.vector_norm(D))
+            ref = out["dd"][0]
+            for meth in ("native", "split", "dd"):
+                C, ms = out[meth]
+                err = float(torch.linalg.vector_norm(C - ref)) / den
+                by = 2 * M * K * 8
+                rows.append({"M": M, "N": M, "K": K, "method": meth, "ms": round(ms, 3),
+                             "GB/s": round(by / (ms * 1e-3) / 1e9, 1),
+                             "eff_fp64_tflops": round(2 * M * M * K / (ms * 1e-3) / 1e12, 2),
+                             "normwise_err_vs_dd": err if meth != "dd" else 0.0})
+            for r in rows[-3:]:
+                r["speedup_vs_native"] = round(out["native"][1] / r["ms"], 2)
+            del A, B, D, out
+            torch.cuda.empty_cache()
+    launches = L.skinny_kernel_launches() - n0
+    h.check_device()
+    value = total_bytes / (total_ms * 1e-3) / 1e9
+    if rank == 0:
+        split = {r["M"]: r for r in rows if r["method"] == "split"}
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(total_ms / max(1, args.steps), 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic s*2^e (s U[1,2), random sign, e U{-20..20}) from a seeded generator",
+                "config": {"workload": "precision-c3", "description": WORKLOADS["precision-c3"][1],
+                           "l2": "operands larger than L2 (no flush needed)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "tensor", "kernel": "split_wide_kernel",
+                             "achieved_eff_fp64_tflops": round(sum(split[m]["eff_fp64_tflops"] for m in split) / 3, 2),
+                             "hbm_GB/s": round(value, 1), "hbm_peak": hbm, "hbm_frac": round(value / hbm, 4),
+                             "note": "value = algorithmic bytes of the split launches / their time"},
+                "split_vs_fp64": {str(m): {"speedup": split[m]["speedup_vs_native"],
+                                           "err": split[m]["normwise_err_vs_dd"]} for m in split},
+                "precision": rows, "gpu_launches": int(launches), "clocks": clk.summary(),
+                "cpu_baseline": None, "e2e": None}
+        print(json.dumps(line), flush=True)
+    h.close()
 
 
 def measure_e2e(h, items, ops, args, world):
