@@ -142,6 +142,13 @@ def c4_items():
                  flops=4 * M * M * K, copies=1) for M in (16, 32, 64)]
 
 
+def c5_items():
+    reqs = c5_requests(200, 2024)
+    return [dict(op=r["op"] if r["op"] != "svqb" else "tsmttsm", dt=r["dt"] if r["dt"] != "f32" else "f64",
+                 M=r["M"], N=r["N"], K=r["K"] // 16 * 16 or 16, inplace=False, s=r["s"] if r["dt"] != "f32" else 8,
+                 bytes=r["bytes"], flops=0) for r in reqs[:20]]
+
+
 def probe_tsmm_items():
     M = N = 8
     K = 1 << 22
@@ -180,6 +187,9 @@ WORKLOADS = {
                    "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
     "tsmttsm-c1": (c1_items, "TSMTTSM FP64 C(8x8) = A^T B, K = 2^20, alpha 1, beta 0, "
                    "16 rotating input copies (2 GiB > L2)"),
+    "serve-c5": (c5_items, "Poisson stream of TSMTTSM 50% / TSMM 35% / SVQB 15% requests, K log-uniform "
+                 "[2^14, 2^24], M, N in {1..64}, FP64 60% / complex FP64 25% / FP32 15%, operands resident in "
+                 "HBM; request loop vs one launch per call"),
     "svqb-c4": (c4_items, "SVQB of X (K = 2^24, M in {16, 32, 64}, condition 1e8), Gram in plain FP64, split "
                 "precision or double-double; time and ||Q^T Q - I||_F"),
     "precision-c3": (c3_items, "TSMTTSM FP64 M = N in {32, 64, 128}, K = 2^24, entries s*2^e, plain FP64 vs "
@@ -339,6 +349,8 @@ def main():
     ap.add_argument("--method", default="auto", choices=["auto", "native", "split", "dd"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--requests", type=int, default=2000, help="serve-c5: number of requests")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve-c5: Poisson arrival rate per second")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -346,6 +358,8 @@ def main():
         return run_precision(args)
     if args.workload == "svqb-c4":
         return run_svqb(args)
+    if args.workload == "serve-c5":
+        return run_serve(args)
 
     import torch
     from skinny_matmul_gb300 import Handle, build, lib
@@ -445,6 +459,198 @@ def main():
 
 # DRAM bytes per step of the dominant kernel from one ncu capture (profiles/), or None.
 TRAFFIC = {}
+
+
+# ------------------------------------------------------------------------------ serving (C5)
+C5_WIDTHS = (1, 2, 4, 8, 16, 32, 64)
+
+
+def c5_requests(n, seed):
+    """The serving mix: TSMTTSM 50 %, TSMM 35 %, SVQB 15 %; K log-uniform in [2^14, 2^24]; M, N
+    from {1, 2, 4, 8, 16, 32, 64}; FP64 60 %, complex FP64 25 %, FP32 15 % (SVQB: FP64)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(n):
+        op = str(rng.choice(["tsmttsm", "tsmm", "svqb"], p=[0.5, 0.35, 0.15]))
+        dt = str(rng.choice(["f64", "c64", "f32"], p=[0.6, 0.25, 0.15]))
+        if op == "svqb":
+            dt = "f64"
+        K = int(2 ** rng.uniform(14, 24))
+        M = int(rng.choice(C5_WIDTHS))
+        N = M if op == "svqb" else int(rng.choice(C5_WIDTHS))
+        s = {"f64": 8, "c64": 16, "f32": 4}[dt]
+        if op == "tsmttsm":
+            by = (M + N) * K * s
+        elif op == "tsmm":
+            by = (M * K + N * K + M * N) * s  # beta = 0
+        else:
+            by = 3 * K * M * 8
+        reqs.append(dict(op=op, dt=dt, K=K, M=M, N=N, s=s, bytes=by, u=float(rng.random()), v=float(rng.random())))
+    return reqs
+
+
+class C5Pools:
+    """Operands resident in HBM: one FP64 pool (read as FP64 or interleaved complex FP64), one FP32
+    pool, an SVQB pool (updated in place), and output scratch.  A request reads a slice of a pool at
+    a seeded offset; outputs (alpha = 1, beta = 0) go to scratch that no request reads."""
+
+    def __init__(self, dev, seed):
+        import torch
+        g = torch.Generator(device=dev).manual_seed(seed)
+        self.kmax = 1 << 24
+        n64 = self.kmax * 64 * 2 + (1 << 20)
+        self.p64 = torch.rand(n64, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+        self.p32 = torch.rand(self.kmax * 64 + (1 << 20), dtype=torch.float32, device=dev, generator=g) * 2 - 1
+        self.psv = torch.randn(self.kmax * 64 * 3, dtype=torch.float64, device=dev, generator=g)
+        self.out = torch.empty(self.kmax * 64 * 2, dtype=torch.float64, device=dev)
+        self.outs = torch.empty(1 << 16, dtype=torch.float64, device=dev)
+
+    def slice(self, pool, count, u):
+        off = int(u * (pool.numel() - count)) & ~255
+        return pool[off:off + count]
+
+    def operands(self, r):
+        """(A, B, C) device views for request r; element counts in the pool's own type."""
+        M, N, K = r["M"], r["N"], r["K"]
+        w = 2 if r["dt"] == "c64" else 1  # doubles per element
+        if r["op"] == "svqb":
+            X = self.slice(self.psv, K * M, r["u"])
+            return X, None, X
+        pool = self.p32 if r["dt"] == "f32" else self.p64
+        A = self.slice(pool, K * M * w, r["u"])
+        if r["op"] == "tsmttsm":
+            B = self.slice(pool, K * N * w, r["v"])
+            C = self.outs[: M * N * w] if r["dt"] != "f32" else self.outs.view(torch_f32())[: M * N]
+        else:
+            B = self.slice(pool, M * N * w, r["v"])
+            C = self.out[: K * N * w] if r["dt"] != "f32" else self.out.view(torch_f32())[: K * N]
+        return A, B, C
+
+
+def torch_f32():
+    import torch
+    return torch.float32
+
+
+def c5_call(h, r, ops, stream=None):
+    from skinny_matmul_gb300 import lib as SL
+    A, B, C = ops
+    acc = "auto" if r["dt"] == "f64" else "native"
+    dt = {"f64": SL.R64, "c64": SL.C64, "f32": SL.R32}[r["dt"]]
+    if r["op"] == "svqb":
+        h.svqb(r["K"], r["M"], C, r["M"], gram_acc="auto", orth_err=False, stream=stream)
+    elif r["op"] == "tsmttsm":
+        h.tsmttsm(r["M"], r["N"], r["K"], A, r["M"], 1.0, B, r["N"], 0.0, C, r["M"], acc=acc, stream=stream, dtype=dt)
+    else:
+        h.tsmm(r["M"], r["N"], r["K"], A, r["M"], 1.0, B, r["M"], 0.0, C, r["N"], acc=acc, stream=stream, dtype=dt)
+
+
+def run_serve(args):
+    """A seeded Poisson stream of requests on operands resident in HBM, run two ways: through the
+    request loop (continuous batching: admission by a 120 GB budget, up to 16 requests in flight on
+    8 streams) and one launch per call (each request launched when it arrives and waited for before
+    the next, as the reference's drivers call its launchers).  Throughput = algorithmic bytes of all
+    requests / (last completion - first arrival); latency = completion - arrival."""
+    import numpy as np
+    import torch
+    from skinny_matmul_gb300 import Handle, Server, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = args.requests
+    reqs = c5_requests(n, 2024 + rank)
+    pools = C5Pools(dev, 99 + rank)
+    ops = [pools.operands(r) for r in reqs]
+    total_bytes = float(sum(r["bytes"] for r in reqs))
+    rng = np.random.default_rng(7 + rank)
+    gaps = rng.exponential(1.0 / args.rate, n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    # warm-up: every (op, dtype, width) kind once, small K
+    seen = set()
+    for r, o in zip(reqs, ops):
+        key = (r["op"], r["dt"], r["M"], r["N"])
+        if key not in seen:
+            seen.add(key)
+            c5_call(h, dict(r, K=min(r["K"], 1 << 14)), o)
+    torch.cuda.synchronize()
+    h.check_device()
+    n0 = L.skinny_kernel_launches()
+
+    def one_per_call():
+        lat = []
+        t0 = time.perf_counter()
+        for i, (r, o) in enumerate(zip(reqs, ops)):
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            c5_call(h, r, o)
+            torch.cuda.synchronize()
+            lat.append(time.perf_counter() - t0 - arrivals[i])
+        return time.perf_counter() - t0, lat
+
+    def served():
+        srv = Server(h, 120 * (1 << 30), num_streams=8, max_inflight=16)
+        tickets = []
+        t0 = time.perf_counter()
+        for i, (r, o) in enumerate(zip(reqs, ops)):
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            A, B, C = o
+            dt = {"f64": "float64", "c64": "complex128", "f32": "float32"}[r["dt"]]
+            acc = "auto" if r["dt"] == "f64" else "native"
+            if r["op"] == "svqb":
+                st, t = srv.submit("svqb", dt, r["M"], r["M"], r["K"], C, r["M"], None, 0, C, r["M"], 1.0, 0.0, "auto",
+                                   device=True)
+            elif r["op"] == "tsmttsm":
+                st, t = srv.submit("tsmttsm", dt, r["M"], r["N"], r["K"], A, r["M"], B, r["N"], C, r["M"], 1.0, 0.0,
+                                   acc, device=True)
+            else:
+                st, t = srv.submit("tsmm", dt, r["M"], r["N"], r["K"], A, r["M"], B, r["M"], C, r["N"], 1.0, 0.0,
+                                   acc, device=True)
+            if st != lib.OK:
+                raise RuntimeError(f"submit failed: {st}")
+            tickets.append(t)
+        srv.drain(3600.0)
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+        srv.close()
+        return wall, stats
+
+    with ClockSampler(local) as clk:
+        wall_seq, lat_seq = one_per_call()
+        wall_srv, st_srv = served()
+    launches = L.skinny_kernel_launches() - n0
+    h.check_device()
+    lat_seq = sorted(lat_seq)
+    p = lambda v, q: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+    seq = {"GB/s": round(total_bytes / wall_seq / 1e9, 1), "requests_per_s": round(n / wall_seq, 1),
+           "p50_ms": round(p(lat_seq, 0.5) * 1e3, 3), "p99_ms": round(p(lat_seq, 0.99) * 1e3, 3),
+           "wall_s": round(wall_seq, 3)}
+    srv = {"GB/s": round(total_bytes / wall_srv / 1e9, 1), "requests_per_s": round(n / wall_srv, 1),
+           "p50_ms": round(st_srv["p50_latency_us"] / 1e3, 3), "p99_ms": round(st_srv["p99_latency_us"] / 1e3, 3),
+           "wall_s": round(wall_srv, 3), "completed": int(st_srv["completed"]), "failed": int(st_srv["failed"]),
+           "max_inflight_seen": int(st_srv["max_inflight_seen"]),
+           "peak_bytes_in_use": int(st_srv["peak_bytes_in_use"])}
+    value = sum_over_ranks(total_bytes / wall_srv / 1e9, world)
+    if rank == 0:
+        hbm, _ = peaks()
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": 1,
+                "warmup": 1, "ms_per_step": round(wall_srv * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "mixed (f64 60%, c64 25%, f32 15%)",
+                "data": "synthetic U[-1,1) operands resident in HBM, seeded; Poisson arrivals",
+                "config": {"workload": "serve-c5", "description": WORKLOADS["serve-c5"][1], "requests": n,
+                           "arrival_rate_per_s": args.rate, "l2": "operands larger than L2 for most requests",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "hbm", "achieved": round(value, 1), "peak": hbm, "unit": "GB/s",
+                             "frac": round(value / hbm, 4), "traffic": None, "kernel": "request mix"},
+                "serving": {"served": srv, "one_launch_per_call": seq,
+                            "throughput_ratio": round(seq["wall_s"] / wall_srv, 3),
+                            "p99_ratio": round(srv["p99_ms"] / seq["p99_ms"], 3) if seq["p99_ms"] else None},
+                "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": None, "e2e": None}
+        print(json.dumps(line), flush=True)
+    h.close()
 
 
 # --------------------------------------------------------------------------------- SVQB (C4)

@@ -146,7 +146,9 @@ skinny_status skinny_tune_import(skinny_handle handle, const char* json);
  * runs each (upload, product, download) on one of its streams so that the work of requests in
  * flight overlaps on the device, and retires them as their completion events fire; admission
  * continues while others run.  Host buffers must stay valid until the ticket completes; pinned
- * host memory lets uploads and downloads overlap with compute.  A server created with a NULL
+ * host memory lets uploads and downloads overlap with compute.  Requests flagged `device` name
+ * operands already resident in HBM: the server then only schedules them (admission counts their
+ * operand bytes against the budget) and runs the product on them in place.  A server created with a NULL
  * handle runs in dry mode: nothing touches a device and each request "runs" for a time
  * proportional to its bytes (for testing the scheduling logic without a GPU). */
 typedef enum { SKINNY_OP_TSMTTSM = 0, SKINNY_OP_TSMM = 1, SKINNY_OP_SVQB = 2 } skinny_op;
@@ -163,6 +165,8 @@ typedef struct {
   void* C;       /* host; read when beta != 0, always written; SVQB: X */
   int64_t ldc;
   double alpha[2], beta[2]; /* (re, im); real dtypes use [0] */
+  int32_t device; /* 0: A, B, C are host buffers (uploaded and downloaded by the server);
+                     1: device buffers resident in HBM, used in place (nothing copied) */
 } skinny_request;
 
 typedef struct {

@@ -173,7 +173,8 @@ class Server:
     """Request loop with continuous batching (skinny_server_* in include/skinny.h).
 
     Requests carry HOST numpy buffers (keep them alive until the ticket completes; pinned memory
-    overlaps transfers).  handle=None runs the scheduler in dry mode (no device work)."""
+    overlaps transfers) or, with device=True, device tensors resident in HBM.  handle=None runs
+    the scheduler in dry mode (no device work)."""
 
     def __init__(self, handle: Handle | None, mem_budget_bytes: int, num_streams: int = 4,
                  max_inflight: int = 16):
@@ -185,13 +186,16 @@ class Server:
         self._keep = {}
 
     def submit(self, op, dtype, M, N, K, A, lda, B=None, ldb=0, C=None, ldc=0, alpha=1.0, beta=0.0,
-               acc="native"):
-        """Queue a request; returns its ticket.  A, B, C are host arrays (numpy) or addresses."""
+               acc="native", device=False):
+        """Queue a request; returns its ticket.  A, B, C are host arrays (numpy) or addresses; with
+        device=True they are device tensors (or device addresses) resident in HBM, used in place."""
         def addr(x):
             if x is None:
                 return None
             if isinstance(x, int):
                 return x
+            if hasattr(x, "data_ptr"):
+                return x.data_ptr()
             return x.ctypes.data
         r = L.Request()
         r.op, r.dtype, r.acc = _OPS[op], _DT[dtype], _ACC[acc]
@@ -199,6 +203,7 @@ class Server:
         r.A, r.lda, r.B, r.ldb, r.C, r.ldc = addr(A), lda, addr(B), ldb, addr(C), ldc
         a, b = complex(alpha), complex(beta)
         r.alpha[0], r.alpha[1], r.beta[0], r.beta[1] = a.real, a.imag, b.real, b.imag
+        r.device = 1 if device else 0
         t = ctypes.c_uint64()
         st = self.lib.skinny_server_submit(self.s, ctypes.byref(r), ctypes.byref(t))
         if st == L.OK:

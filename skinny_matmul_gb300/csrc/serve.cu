@@ -10,7 +10,9 @@
 //     the result is downloaded, all on one of the server's streams (round-robin), followed by a
 //     completion event -- requests in flight on different streams overlap on the device;
 //   * completions are retired by polling their events; retiring frees the buffers (stream-ordered)
-//     and returns their bytes to the budget, which admits the next requests while others run.
+//     and returns their bytes to the budget, which admits the next requests while others run;
+//   * requests on operands resident in HBM (device flag) skip the buffers and copies: their
+//     operand bytes count against the budget while they run, and the product runs in place.
 // Dry mode (no handle) replaces the device work by a delay proportional to the request's bytes so
 // the admission, ticket and accounting logic can be exercised without a GPU.
 #include <cuda_runtime.h>
@@ -126,6 +128,25 @@ void skinny_server_st::start_job(Job* j) {
   j->stream = streams[rr++ % streams.size()];
   cudaStream_t st = j->stream;
   const size_t s = esize(r.dtype);
+  // scalars in the request are doubles; single-precision dtypes take floats
+  const bool single = r.dtype == SKINNY_R32 || r.dtype == SKINNY_C32;
+  const float af[2] = {(float)r.alpha[0], (float)r.alpha[1]}, bf[2] = {(float)r.beta[0], (float)r.beta[1]};
+  const void* al = single ? (const void*)af : (const void*)r.alpha;
+  const void* be = single ? (const void*)bf : (const void*)r.beta;
+  if (r.device) {  // operands resident in HBM: run in place
+    if (r.op == SKINNY_OP_TSMTTSM)
+      j->status = product(h, false, r.dtype, r.acc, r.M, r.N, r.K, r.A, r.lda, al, r.B, r.ldb, be, r.C, r.ldc, st,
+                          nullptr);
+    else if (r.op == SKINNY_OP_TSMM)
+      j->status = product(h, true, r.dtype, r.acc, r.M, r.N, r.K, r.A, r.lda, al, r.B, r.ldb, be, r.C, r.ldc, st,
+                          nullptr);
+    else
+      j->status = skinny_svqb(h, r.acc, r.K, r.M, (double*)(r.C ? r.C : const_cast<void*>(r.A)), r.lda, nullptr, st);
+    if (cudaGetLastError() != cudaSuccess && j->status == SKINNY_OK) j->status = SKINNY_DEVICE_ERROR;
+    cudaEventCreateWithFlags(&j->done, cudaEventDisableTiming);
+    cudaEventRecord(j->done, st);
+    return;
+  }
   auto fail = [&](skinny_status why, const char* msg) {
     if (j->status == SKINNY_OK) j->status = why;
     set_error(msg);
@@ -134,11 +155,6 @@ void skinny_server_st::start_job(Job* j) {
   if (j->bB && cudaMallocAsync(&j->dB, j->bB, st) != cudaSuccess) fail(SKINNY_NO_MEM, "serve: allocation");
   if (j->bC && cudaMallocAsync(&j->dC, j->bC, st) != cudaSuccess) fail(SKINNY_NO_MEM, "serve: allocation");
   cudaGetLastError();
-  // scalars in the request are doubles; single-precision dtypes take floats
-  const bool single = r.dtype == SKINNY_R32 || r.dtype == SKINNY_C32;
-  const float af[2] = {(float)r.alpha[0], (float)r.alpha[1]}, bf[2] = {(float)r.beta[0], (float)r.beta[1]};
-  const void* al = single ? (const void*)af : (const void*)r.alpha;
-  const void* be = single ? (const void*)bf : (const void*)r.beta;
   if (j->status == SKINNY_OK) {
     void* dB = j->bB ? j->dB : j->dA;
     void* dC = j->bC ? j->dC : j->dA;

@@ -71,6 +71,7 @@ constexpr uint32_t SLOT = SLOT_A + 2 * LBO_B;  // 43008
 constexpr uint32_t RAW_OP = ROWS * W * 8;      // one operand of an FP64 stage
 constexpr int HDR = 4096;
 constexpr int MAX_EPOCH_PERIODS = 1 << 14;     // int64 words hold 2^15 periods of < 2^48.1
+constexpr int GROUP = 16;                      // chunks per first-level group of the finish (<= 15 groups)
 
 struct Args {
   const double* A;
@@ -85,8 +86,8 @@ struct Args {
   int rstages;
   uint32_t raw_stage;  // bytes per FP64 stage
   int64_t nstages;     // ceil(K / ROWS)
-  double* partials;    // [nblk][nchunks][2][4096]
-  unsigned* counter;   // one ticket per block
+  double* partials;    // [nblk][nchunks][2][4096], then [nblk][15][4096] group sums
+  unsigned* counter;   // tickets: [nblk][16] (15 groups + the block)
   int* err;
 };
 
@@ -149,12 +150,6 @@ __device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile
   *ab = 1;
   if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
   return false;
-}
-
-__device__ __forceinline__ uint32_t exp_field(double x) {
-  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  const uint32_t ef = (hi >> 20) & 0x7FF;
-  return ((hi & 0x7FFFFFFFu) | lo) ? (ef ? ef : 1u) : 0u;
 }
 
 // signed fixed-point value of x relative to exponent field E, offset for balanced base-256 digits
@@ -371,19 +366,24 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       }
       flushed = true;
     };
-    auto drain = [&](int buf) {
-      const int ep = rec_epoch[buf];
-      if (ep != acc_epoch) {  // uniform: a new epoch begins with this period
-        flush();
-        slicers_sync();
-        if (tid < 128) acc_rec[tid] = rec[buf * 128 + tid];
-        slicers_sync();
-        acc_epoch = ep;
+    // drain piece k (cells 8k..8k+7 of this thread) of the TMEM set `buf`; piece 0 first closes
+    // the accumulators' epoch when the period belongs to a new one
+    auto drain_piece = [&](int buf, int k) {
+      if (k == 0) {
+        const int ep = rec_epoch[buf];
+        if (ep != acc_epoch) {  // uniform: a new epoch begins with this period
+          flush();
+          slicers_sync();
+          if (tid < 128) acc_rec[tid] = rec[buf * 128 + tid];
+          slicers_sync();
+          acc_epoch = ep;
+        }
       }
       tc_after();
       const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + buf * 256 + 32 * nh;
 #pragma unroll
       for (int hp = 0; hp < 4; hp++) {
+        if (hp != k) continue;
         uint32_t s0[8], s1[8], s2[8], s3[8];
         tmem_ld8(tb + hp * 8, s0);          // key 2, columns j   : level 2 / 6
         tmem_ld8(tb + 64 + hp * 8, s1);     // key 2, columns j+1 : level 3 / 7
@@ -403,40 +403,58 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     };
 
     int cur_buf = 1, pstart = 0, epoch = 0, epoch_periods = 0;
-    int pend = 0, pend_buf = 0, pend_last = 0;
+    // the period before the current one is drained in 4 pieces over the stages that follow the
+    // completion of its last MMAs, so that the conversions interleave with slicing
+    int pend = 0, pend_buf = 0, pend_last = 0, pend_piece = 0;
     for (int ls = 0; ls < nst; ls++) {
       const int rs = ls % R, ds = ls % DSLOTS;
       const int64_t row0 = (s_begin + ls) * ROWS;
       const int rows = (int)min((int64_t)ROWS, p.K - row0);
       wait_ab(&raw_full[rs], (uint32_t)((ls / R) & 1), abort_f, p.err);
-      if (ls >= DSLOTS) wait_ab(&dempty[ds], (uint32_t)(((ls / DSLOTS) - 1) & 1), abort_f, p.err);
+      // slot reuse: lane 0 waits for the MMAs that read the slot, then the warp writes it
+      if (ls >= DSLOTS && lane == 0) wait_ab(&dempty[ds], (uint32_t)(((ls / DSLOTS) - 1) & 1), abort_f, p.err);
+      __syncwarp();
       // load my unit and its column maximum
       const double* T = reinterpret_cast<const double*>(raw + (size_t)rs * p.raw_stage) + (isB ? ROWS * W : 0);
       const int rstr = isB ? rsb : rsa;
+      // column maximum of |x| from the high words (the exponent field of the largest high word is
+      // the largest exponent field); nonzero low words mark subnormals in an otherwise zero column
       double v[8];
-      uint32_t e = 0;
+      uint32_t mh = 0, ol = 0;
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         const int rr = sub * nrow + k;
         v[k] = (k < nrow && cvalid && rr < rows) ? T[rr * rstr + c] : 0.0;
-        e = max(e, exp_field(v[k]));
+        mh = max(mh, (uint32_t)__double2hiint(v[k]) & 0x7FFFFFFFu);
+        ol |= (uint32_t)__double2loint(v[k]);
       }
-      if (gram) e = max(e, __shfl_xor_sync(0xffffffffu, e, 8));
-      e = max(e, __shfl_xor_sync(0xffffffffu, e, 16));
+      if (gram) {
+        mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, 8));
+        ol |= __shfl_xor_sync(0xffffffffu, ol, 8);
+      }
+      mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, 16));
+      ol |= __shfl_xor_sync(0xffffffffu, ol, 16);
+      uint32_t e = mh >> 20;
+      if (e == 0 && (mh | ol)) e = 1;
       __syncwarp();
       if (lane == 0) mbar_arrive(&raw_empty[rs]);
       const int bump = slicers_any(e > Ecur);
       const bool start = ls == 0 || bump || ls - pstart >= PSTAGES || epoch_periods >= MAX_EPOCH_PERIODS;
       if (start) {
-        if (pend) {  // the period before the current one still holds its TMEM set: drain it now
-          wait_ab(&dempty[pend_last % DSLOTS], (uint32_t)((pend_last / DSLOTS) & 1), abort_f, p.err);
-          drain(pend_buf);
+        if (pend) {  // the period before the current one still holds its TMEM set: finish it now
+          // its last MMAs: waited on already once its slot was reused (ls >= pend_last + DSLOTS);
+          // before that the slot's barrier has not moved past that phase, so the parity wait holds
+          if (ls < pend_last + DSLOTS && lane == 0)
+            wait_ab(&dempty[pend_last % DSLOTS], (uint32_t)((pend_last / DSLOTS) & 1), abort_f, p.err);
+          __syncwarp();
+          for (int k = pend_piece; k < 4; k++) drain_piece(pend_buf, k);
           pend = 0;
         }
         if (ls > 0) {
           pend = 1;
           pend_buf = cur_buf;
           pend_last = ls - 1;
+          pend_piece = 0;
         }
         cur_buf ^= 1;
         pstart = ls;
@@ -451,10 +469,10 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
           if (gram) rec[cur_buf * 128 + 64 + c] = (int)Ecur;
         }
         if (tid == 0) rec_epoch[cur_buf] = epoch;
-      } else if (pend && ls == pend_last + DSLOTS) {
+      } else if (pend && ls >= pend_last + DSLOTS) {
         // the MMAs of the pending period's last stage are complete (waited on for slot reuse)
-        drain(pend_buf);
-        pend = 0;
+        drain_piece(pend_buf, pend_piece);
+        if (++pend_piece == 4) pend = 0;
       }
       if (tid == 0) flags[ds] = (start ? 1 : 0) | (cur_buf << 1);
       // slice: digits relative to Ecur into slot ds
@@ -514,14 +532,25 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     }
     // last periods
     if (pend) {
-      wait_ab(&dempty[pend_last % DSLOTS], (uint32_t)((pend_last / DSLOTS) & 1), abort_f, p.err);
-      drain(pend_buf);
+      if (nst - 1 < pend_last + DSLOTS && lane == 0)  // no processed stage reused its slot
+        wait_ab(&dempty[pend_last % DSLOTS], (uint32_t)((pend_last / DSLOTS) & 1), abort_f, p.err);
+      __syncwarp();
+      for (int k = pend_piece; k < 4; k++) drain_piece(pend_buf, k);
     }
     if (nst > 0) {
-      wait_ab(&dempty[(nst - 1) % DSLOTS], (uint32_t)(((nst - 1) / DSLOTS) & 1), abort_f, p.err);
-      drain(cur_buf);
+      if (lane == 0)
+        wait_ab(&dempty[(nst - 1) % DSLOTS], (uint32_t)(((nst - 1) / DSLOTS) & 1), abort_f, p.err);
+      __syncwarp();
+      for (int k = 0; k < 4; k++) drain_piece(cur_buf, k);
     }
     flush();
+    // the CTA's sum of a cell: levels 2..5 (half 0) plus levels 6..9 (half 1), into half 0
+    slicers_sync();
+    if (hm == 0 && m < Mb)
+      for (int x = 0; x < 32; x++) {
+        const int n = 32 * nh + x;
+        if (n < Nb) part[n * 64 + m] += part[4096 + n * 64 + m];
+      }
   }
 
   tc_before();
@@ -529,22 +558,48 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
   if (*abort_f) return;
 
-  // ---- cross-CTA finish: the last CTA of the block sums the chunks in order ----------------------
+  // ---- cross-CTA finish, two levels: the last CTA of each group of GROUP chunks sums the group's
+  // partials in chunk order; the last group to finish sums the group sums in group order and
+  // applies alpha and beta (deterministic; the work is spread over the group finishers) -----------
   __threadfence();
   __syncthreads();
   __shared__ int s_last;
-  if (tid == 0) s_last = (atomicAdd(p.counter + blk, 1u) == (unsigned)(nchunks - 1));
+  const int ngroups = (nchunks + GROUP - 1) / GROUP, grp = chunk / GROUP;
+  const int gsize = min(GROUP, nchunks - grp * GROUP);
+  unsigned* gcount = p.counter + blk * 16;  // [grp] per group, [15] for the block
+  if (tid == 0) s_last = (atomicAdd(gcount + grp, 1u) == (unsigned)(gsize - 1));
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  const double* P = p.partials + (size_t)blk * nchunks * 2 * 4096;
+  const double* P = p.partials + (size_t)blk * nchunks * 8192;           // [chunk][2][4096], half 0 = CTA sum
+  double* G = p.partials + (size_t)gridDim.x * 8192 + (size_t)blk * 15 * 4096;  // [group][4096]
   for (int e = tid; e < Mb * Nb; e += THREADS) {
-    const int mm = e % Mb, nn = e / Mb;
+    const int cell = (e / Mb) * 64 + e % Mb;
+    double v[GROUP];
+#pragma unroll
+    for (int i = 0; i < GROUP; i++) v[i] = i < gsize ? __ldcg(P + (size_t)(grp * GROUP + i) * 8192 + cell) : 0.0;
     double sum = 0.0;
-    for (int ch = 0; ch < nchunks; ch++) {
-      sum += __ldcg(P + ((size_t)ch * 2) * 4096 + nn * 64 + mm);
-      sum += __ldcg(P + ((size_t)ch * 2 + 1) * 4096 + nn * 64 + mm);
-    }
+#pragma unroll
+    for (int i = 0; i < GROUP; i++) sum += v[i];
+    G[(size_t)grp * 4096 + cell] = sum;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    gcount[grp] = 0u;
+    s_last = (atomicAdd(gcount + 15, 1u) == (unsigned)(ngroups - 1));
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int e = tid; e < Mb * Nb; e += THREADS) {
+    const int mm = e % Mb, nn = e / Mb, cell = nn * 64 + mm;
+    double v[15];
+#pragma unroll
+    for (int i = 0; i < 15; i++) v[i] = i < ngroups ? __ldcg(G + (size_t)i * 4096 + cell) : 0.0;
+    double sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < 15; i++) sum += v[i];
     double* cc = p.C + (int64_t)(W * bj + nn) * p.ldc + W * bi + mm;
     *cc = p.beta_zero ? p.alpha * sum : (*cc) * p.beta + sum * p.alpha;
     if (p.sym && bi < bj) {  // Gram: the mirrored block holds the same sums
@@ -552,7 +607,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       *cm = p.beta_zero ? p.alpha * sum : (*cm) * p.beta + sum * p.alpha;
     }
   }
-  if (tid == 0) p.counter[blk] = 0u;
+  if (tid == 0) gcount[15] = 0u;
 }
 
 }  // namespace splitw
@@ -593,10 +648,11 @@ skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const
   }
   const int smem = (int)(fixed + (int64_t)a.rstages * a.raw_stage);
   a.nstages = (K + ROWS - 1) / ROWS;
-  const int64_t nchunks = std::max<int64_t>(1, std::min<int64_t>(a.nstages, h->dev.sms / a.nblk));
+  const int64_t nchunks = std::max<int64_t>(1, std::min<int64_t>({a.nstages, h->dev.sms / a.nblk,
+                                                                   (int64_t)15 * GROUP}));
   const int64_t grid = nchunks * a.nblk;
   Workspace& ws = h->ws[st];
-  skinny_status s = workspace_ensure(ws, (size_t)grid * 2 * 4096 * 8, st);
+  skinny_status s = workspace_ensure(ws, ((size_t)grid * 2 + (size_t)a.nblk * 15) * 4096 * 8, st);
   if (s != SKINNY_OK) return s;
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;

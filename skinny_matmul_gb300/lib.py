@@ -34,7 +34,7 @@ class Request(ctypes.Structure):
                 ("M", ctypes.c_int64), ("N", ctypes.c_int64), ("K", ctypes.c_int64),
                 ("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
                 ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64),
-                ("alpha", ctypes.c_double * 2), ("beta", ctypes.c_double * 2)]
+                ("alpha", ctypes.c_double * 2), ("beta", ctypes.c_double * 2), ("device", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):

@@ -113,3 +113,31 @@ def test_served_results_match_oracle(handle):
         assert common.normwise(C, exp, den, common.c_mask_tsmttsm(r["M"], r["N"], r["ldc"])) <= \
             common.tol(np.float64, r["K"])
     srv.close()
+
+
+def test_device_resident_requests_identical_to_alone(handle):
+    """Requests on operands resident in HBM (device flag): the server runs them in place, several
+    in flight; every result equals the same request run alone."""
+    reqs = make_requests(23, 40)
+    expected = [run_alone(handle, r) for r in reqs]
+    srv = Server(handle, 8 << 30, num_streams=4, max_inflight=8)
+    outs, tickets = [], []
+    for r in reqs:
+        A = torch.from_numpy(r["A"].copy()).cuda()
+        if r["op"] == "svqb":
+            B, C = None, A
+        else:
+            B = A if r["B"] is r["A"] else torch.from_numpy(r["B"].copy()).cuda()
+            C = A if r["C"] is r["A"] else torch.from_numpy(r["C"].copy()).cuda()
+        outs.append((A, B, C))
+        st, t = srv.submit(r["op"], r["dtype"], r["M"], r["N"], r["K"], A, r["lda"], B, r["ldb"], C, r["ldc"],
+                           r["alpha"], r["beta"], r["acc"], device=True)
+        assert st == L.OK
+        tickets.append(t)
+    for t in tickets:
+        assert srv.wait(t, 120) == (L.OK, L.OK)
+    stats = srv.stats()
+    assert stats["completed"] == len(reqs) and stats["max_inflight_seen"] >= 2
+    for (A, B, C), r, e in zip(outs, reqs, expected):
+        assert np.array_equal(C.cpu().numpy(), e), (r["op"], r["dtype"], r["M"], r["N"], r["K"])
+    srv.close()
