@@ -58,3 +58,18 @@ def test_launcher_list_shape():
         for dt in ("float32", "float64", "complex64", "complex128", "dd"):
             ls = launchers(op, dt)
             assert len(ls) == 1 and callable(ls[0][0]) and isinstance(ls[0][1], str)
+
+
+def test_cpp_shim_header_compiles():
+    """include/skinny.hpp (the reference's launcher spellings) compiles as C++17 against the CUDA
+    headers, together with the driver the GPU test runs."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers are missing")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", os.path.join(root, "include"), "-I", cuda_inc,
+                        os.path.join(root, "tests", "cpp", "shim_driver.cpp")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
