@@ -8,7 +8,12 @@ M = N in {1,2,4,8,16,32,64} plus (M,N) in {(4,16),(16,4),(8,32)}, K chosen so A 
 in-place form (C = A) for every M = N; entries U[-1,1) from a seeded generator.  One step runs every
 shape once.  Each shape's operands are larger than L2 (129 MB), so no L2 flush is needed.
 
-Other workloads: "tsmttsm-c1" (TSMTTSM FP64 8x8, K = 2^20, 16 rotating input copies).
+The default line also carries "split_vs_fp64" (TSMTTSM FP64 64x64, K = 2^24, s*2^e entries: plain
+FP64 vs split precision vs double-double, with errors) and "serving" (600 requests of the serving
+mix through the request loop vs one launch per call); --no-extras skips them.
+
+Other workloads: "tsmttsm-c1" (TSMTTSM FP64 8x8, K = 2^20, 16 rotating input copies),
+"precision-c3" (M = N in {32, 64, 128}), "svqb-c4", "serve-c5" (2000 requests), and probes for ncu.
 
 Byte and flop formulas follow the reference's perf harness (perf.cu:208-232):
   TSMM beta != 0: (M K + 2 N K + M N) s bytes, in place (M K + N K + M N) s; flops (MNK + NK) f
@@ -226,7 +231,8 @@ def make_operands(it, device, seed):
 
 def call(h, it, ops, i, method):
     M, N, K = it["M"], it["N"], it["K"]
-    acc = method if it["dt"] == "f64" else "native"
+    # FP64 and complex FP64 take the method (split covers complex TSMM); dd is real FP64 only
+    acc = method if it["dt"] == "f64" or (it["dt"] == "c64" and method != "dd") else "native"
     if it["op"] == "tsmm":
         ld_c = M if it["inplace"] else N
         h.tsmm(M, N, K, ops["A"][0], M, 1.0, ops["B"][0], M, 0.5, ops["C"], ld_c, acc=acc)
@@ -350,6 +356,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=2000, help="serve-c5: number of requests")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the compact split-vs-FP64 and serving measurements")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve-c5: Poisson arrival rate per second")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -439,6 +447,26 @@ def main():
         v, cores, desc = cpu_sample(items)
         cpu = {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port", "sample": desc}
 
+    # the metric's other two parts, measured compactly beside the sweep on the same GPU: split vs
+    # plain FP64 TSMTTSM (M = N = 64, K = 2^24, s*2^e data) and the served stream (600 requests)
+    extras = {}
+    if args.workload == "tsmm-sweep" and world == 1 and not args.no_extras:
+        del ops
+        torch.cuda.empty_cache()
+        rows, _, _ = precision_rows(h, dev, (64,), 3, 2, rank, world)
+        byk = {r["method"]: r for r in rows}
+        extras["split_vs_fp64"] = {
+            "config": "TSMTTSM FP64 M = N = 64, K = 2^24, entries s*2^e (e in [-20, 20]); errors normwise "
+                      "against the double-double result",
+            "native_ms": byk["native"]["ms"], "split_ms": byk["split"]["ms"], "dd_ms": byk["dd"]["ms"],
+            "speedup": byk["split"]["speedup_vs_native"], "split_err": byk["split"]["normwise_err_vs_dd"],
+            "native_err": byk["native"]["normwise_err_vs_dd"]}
+        seq, srv, _, wall_srv = serve_measure(h, dev, 600, 2000.0, rank)
+        extras["serving"] = {
+            "config": "600 requests of the serving mix (Poisson, 2000/s), operands resident in HBM",
+            "served": srv, "one_launch_per_call": seq, "throughput_ratio": round(seq["wall_s"] / wall_srv, 3),
+            "p99_ratio": round(srv["p99_ms"] / seq["p99_ms"], 3) if seq["p99_ms"] else None}
+
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
@@ -449,6 +477,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk.summary(), "sweep": per}
+        line.update(extras)
         print(json.dumps(line), flush=True)
     h.check_device()
     h.close()
@@ -536,7 +565,7 @@ def torch_f32():
 def c5_call(h, r, ops, stream=None):
     from skinny_matmul_gb300 import lib as SL
     A, B, C = ops
-    acc = "auto" if r["dt"] == "f64" else "native"
+    acc = "auto" if r["dt"] != "f32" else "native"
     dt = {"f64": SL.R64, "c64": SL.C64, "f32": SL.R32}[r["dt"]]
     if r["op"] == "svqb":
         h.svqb(r["K"], r["M"], C, r["M"], gram_acc="auto", orth_err=False, stream=stream)
@@ -546,27 +575,17 @@ def c5_call(h, r, ops, stream=None):
         h.tsmm(r["M"], r["N"], r["K"], A, r["M"], 1.0, B, r["M"], 0.0, C, r["N"], acc=acc, stream=stream, dtype=dt)
 
 
-def run_serve(args):
-    """A seeded Poisson stream of requests on operands resident in HBM, run two ways: through the
-    request loop (continuous batching: admission by a 120 GB budget, up to 16 requests in flight on
-    8 streams) and one launch per call (each request launched when it arrives and waited for before
-    the next, as the reference's drivers call its launchers).  Throughput = algorithmic bytes of all
-    requests / (last completion - first arrival); latency = completion - arrival."""
+def serve_measure(h, dev, n, rate, rank):
+    """Run the C5 stream both ways; returns (one-per-call stats, served stats, bytes, served wall)."""
     import numpy as np
     import torch
-    from skinny_matmul_gb300 import Handle, Server, build, lib
-    rank, world, local = dist_setup(args.gpus)
-    build.build()
-    h = Handle(torch.cuda.current_device())
-    L = lib.load()
-    dev = torch.device("cuda", torch.cuda.current_device())
-    n = args.requests
+    from skinny_matmul_gb300 import Server, lib
     reqs = c5_requests(n, 2024 + rank)
     pools = C5Pools(dev, 99 + rank)
     ops = [pools.operands(r) for r in reqs]
     total_bytes = float(sum(r["bytes"] for r in reqs))
     rng = np.random.default_rng(7 + rank)
-    gaps = rng.exponential(1.0 / args.rate, n)
+    gaps = rng.exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
     # warm-up: every (op, dtype, width) kind once, small K
     seen = set()
@@ -577,7 +596,6 @@ def run_serve(args):
             c5_call(h, dict(r, K=min(r["K"], 1 << 14)), o)
     torch.cuda.synchronize()
     h.check_device()
-    n0 = L.skinny_kernel_launches()
 
     def one_per_call():
         lat = []
@@ -599,7 +617,7 @@ def run_serve(args):
                 pass
             A, B, C = o
             dt = {"f64": "float64", "c64": "complex128", "f32": "float32"}[r["dt"]]
-            acc = "auto" if r["dt"] == "f64" else "native"
+            acc = "auto" if r["dt"] != "f32" else "native"
             if r["op"] == "svqb":
                 st, t = srv.submit("svqb", dt, r["M"], r["M"], r["K"], C, r["M"], None, 0, C, r["M"], 1.0, 0.0, "auto",
                                    device=True)
@@ -618,11 +636,8 @@ def run_serve(args):
         srv.close()
         return wall, stats
 
-    with ClockSampler(local) as clk:
-        wall_seq, lat_seq = one_per_call()
-        wall_srv, st_srv = served()
-    launches = L.skinny_kernel_launches() - n0
-    h.check_device()
+    wall_seq, lat_seq = one_per_call()
+    wall_srv, st_srv = served()
     lat_seq = sorted(lat_seq)
     p = lambda v, q: v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
     seq = {"GB/s": round(total_bytes / wall_seq / 1e9, 1), "requests_per_s": round(n / wall_seq, 1),
@@ -633,6 +648,31 @@ def run_serve(args):
            "wall_s": round(wall_srv, 3), "completed": int(st_srv["completed"]), "failed": int(st_srv["failed"]),
            "max_inflight_seen": int(st_srv["max_inflight_seen"]),
            "peak_bytes_in_use": int(st_srv["peak_bytes_in_use"])}
+    del pools, ops
+    torch.cuda.empty_cache()
+    return seq, srv, total_bytes, wall_srv
+
+
+def run_serve(args):
+    """A seeded Poisson stream of requests on operands resident in HBM, run two ways: through the
+    request loop (continuous batching: admission by a 120 GB budget, up to 16 requests in flight on
+    8 streams) and one launch per call (each request launched when it arrives and waited for before
+    the next, as the reference's drivers call its launchers).  Throughput = algorithmic bytes of all
+    requests / (last completion - first arrival); latency = completion - arrival."""
+    import numpy as np
+    import torch
+    from skinny_matmul_gb300 import Handle, Server, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = args.requests
+    n0 = L.skinny_kernel_launches()
+    with ClockSampler(local) as clk:
+        seq, srv, total_bytes, wall_srv = serve_measure(h, dev, n, args.rate, rank)
+    launches = L.skinny_kernel_launches() - n0
+    h.check_device()
     value = sum_over_ranks(total_bytes / wall_srv / 1e9, world)
     if rank == 0:
         hbm, _ = peaks()
@@ -741,6 +781,56 @@ def spread_operand(n, gen, device):
     return torch.ldexp(s * sign, e)
 
 
+def precision_rows(h, dev, widths, steps_split, warmup_split, rank, world, K=1 << 24):
+    """Per width M = N: time native, split and dd TSMTTSM on s*2^e data and their normwise errors
+    against the dd result.  Returns (rows, split bytes, split ms)."""
+    import torch
+    rows = []
+    total_bytes, total_ms = 0.0, 0.0
+    for M in widths:
+        g = torch.Generator(device=dev).manual_seed(4242 + M + 13 * rank)
+        A = spread_operand(K * M, g, dev)
+        B = spread_operand(K * M, g, dev)
+        out = {}
+        for meth in ("dd", "native", "split"):
+            C = torch.zeros(M * M, dtype=torch.float64, device=dev)
+            for _ in range(max(1, warmup_split if meth == "split" else 1)):
+                h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
+            steps = steps_split if meth == "split" else max(1, min(steps_split, 2))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            barrier(world)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(steps):
+                h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = max_over_ranks(e0.elapsed_time(e1) / steps, world)
+            out[meth] = (C.clone(), ms)
+            if meth == "split":
+                total_bytes += 2 * M * K * 8 * steps
+                total_ms += ms * steps
+        A.abs_()
+        B.abs_()
+        D = torch.zeros(M * M, dtype=torch.float64, device=dev)
+        h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, D, M, acc="native")
+        den = float(torch.linalg.vector_norm(D))
+        ref = out["dd"][0]
+        for meth in ("native", "split", "dd"):
+            C, ms = out[meth]
+            err = float(torch.linalg.vector_norm(C - ref)) / den
+            by = 2 * M * K * 8
+            rows.append({"M": M, "N": M, "K": K, "method": meth, "ms": round(ms, 3),
+                         "GB/s": round(by / (ms * 1e-3) / 1e9, 1),
+                         "eff_fp64_tflops": round(2 * M * M * K / (ms * 1e-3) / 1e12, 2),
+                         "normwise_err_vs_dd": err if meth != "dd" else 0.0})
+        for r in rows[-3:]:
+            r["speedup_vs_native"] = round(out["native"][1] / r["ms"], 2)
+        del A, B, D, out
+        torch.cuda.empty_cache()
+    return rows, total_bytes, total_ms
+
+
 def run_precision(args):
     """FP64 TSMTTSM C = A^T B at M = N in {32, 64, 128}, K = 2^24, entries s * 2^e, three ways:
     CUDA-core FP64 ("native"), split precision on the tensor cores ("split") and double-double
@@ -754,53 +844,10 @@ def run_precision(args):
     h = Handle(torch.cuda.current_device())
     L = lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
-    K = 1 << 24
-    rows = []
     n0 = L.skinny_kernel_launches()
     hbm, peak_kind = peaks()
-    total_bytes, total_ms = 0.0, 0.0
     with ClockSampler(local) as clk:
-        for M in (32, 64, 128):
-            g = torch.Generator(device=dev).manual_seed(4242 + M + 13 * rank)
-            A = spread_operand(K * M, g, dev)
-            B = spread_operand(K * M, g, dev)
-            out = {}
-            for meth in ("dd", "native", "split"):
-                C = torch.zeros(M * M, dtype=torch.float64, device=dev)
-                for _ in range(max(1, args.warmup if meth == "split" else 1)):
-                    h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
-                steps = args.steps if meth == "split" else max(1, min(args.steps, 2))
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                barrier(world)
-                torch.cuda.synchronize()
-                e0.record()
-                for _ in range(steps):
-                    h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, C, M, acc=meth)
-                e1.record()
-                torch.cuda.synchronize()
-                ms = max_over_ranks(e0.elapsed_time(e1) / steps, world)
-                out[meth] = (C.clone(), ms)
-                if meth == "split":
-                    total_bytes += 2 * M * K * 8 * steps
-                    total_ms += ms * steps
-            A.abs_()
-            B.abs_()
-            D = torch.zeros(M * M, dtype=torch.float64, device=dev)
-            h.tsmttsm(M, M, K, A, M, 1.0, B, M, 0.0, D, M, acc="native")
-            den = float(torch.linalg.vector_norm(D))
-            ref = out["dd"][0]
-            for meth in ("native", "split", "dd"):
-                C, ms = out[meth]
-                err = float(torch.linalg.vector_norm(C - ref)) / den
-                by = 2 * M * K * 8
-                rows.append({"M": M, "N": M, "K": K, "method": meth, "ms": round(ms, 3),
-                             "GB/s": round(by / (ms * 1e-3) / 1e9, 1),
-                             "eff_fp64_tflops": round(2 * M * M * K / (ms * 1e-3) / 1e12, 2),
-                             "normwise_err_vs_dd": err if meth != "dd" else 0.0})
-            for r in rows[-3:]:
-                r["speedup_vs_native"] = round(out["native"][1] / r["ms"], 2)
-            del A, B, D, out
-            torch.cuda.empty_cache()
+        rows, total_bytes, total_ms = precision_rows(h, dev, (32, 64, 128), args.steps, args.warmup, rank, world)
     launches = L.skinny_kernel_launches() - n0
     h.check_device()
     value = total_bytes / (total_ms * 1e-3) / 1e9

@@ -204,16 +204,16 @@ skinny_status tsmttsm_run(const DeviceInfo& dev, Workspace& ws, int* err, cudaSt
 }
 
 // -------------------------------------------------------------------------------------- TSMM
-template <typename T, typename Acc, int TN>
+template <typename T, typename Acc, int TN, int U>
 skinny_status tsmm_launch_tile(const TsmmArgs<T>& a, int bps, int sms, int smem, cudaStream_t st) {
   static std::atomic<int> attr{0};
-  auto kern = tsmm_kernel<T, Acc, TN>;
+  auto kern = tsmm_kernel<T, Acc, TN, U>;
   ensure_smem_attr(kern, smem, attr);
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TSMM_THREADS, smem);
   if (occ < 1) occ = 1;
   if (bps > 0 && bps < occ) occ = bps;
-  const int RS = TSMM_THREADS / a.gn;
+  const int RS = TSMM_THREADS / a.gn * U;
   int64_t need = (a.K + RS - 1) / RS;
   int64_t grid = (int64_t)sms * occ;
   if (grid > need) grid = need;
@@ -261,12 +261,20 @@ skinny_status tsmm_run(const DeviceInfo& dev, cudaStream_t st, int64_t M, int64_
   a.gn = gn;
   a.np = np;
   const int sm = (int)(smem < 16 ? 16 : smem);
+  // narrow rows (M <= 4, a few outputs per thread): 4 rows per thread and step
+  const bool multi = M <= 4 && tn <= 4;
   switch (tn) {
-    case 1: return tsmm_launch_tile<T, Acc, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
-    case 2: return tsmm_launch_tile<T, Acc, 2>(a, o.blocks_per_sm, dev.sms, sm, st);
-    case 4: return tsmm_launch_tile<T, Acc, 4>(a, o.blocks_per_sm, dev.sms, sm, st);
+    case 1:
+      return multi ? tsmm_launch_tile<T, Acc, 1, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
+                   : tsmm_launch_tile<T, Acc, 1, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+    case 2:
+      return multi ? tsmm_launch_tile<T, Acc, 2, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
+                   : tsmm_launch_tile<T, Acc, 2, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+    case 4:
+      return multi ? tsmm_launch_tile<T, Acc, 4, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
+                   : tsmm_launch_tile<T, Acc, 4, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
     default:
-      if constexpr (sizeof(Acc) <= 8) return tsmm_launch_tile<T, Acc, 8>(a, o.blocks_per_sm, dev.sms, sm, st);
+      if constexpr (sizeof(Acc) <= 8) return tsmm_launch_tile<T, Acc, 8, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
   }
   set_error("tsmm: no compiled column tile");
   return SKINNY_UNSUPPORTED;

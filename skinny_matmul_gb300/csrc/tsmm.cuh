@@ -14,8 +14,9 @@
 //     passes __syncwarp(), and only then are outputs written; rows never cross warps, so no
 //     output can overwrite input that another thread still needs.  beta*C reads the element the
 //     same thread then overwrites.
-//   * Rows are distributed grid-stride over a persistent grid; all lanes of a warp run the same
-//     trip count so the __syncwarp() is always reached by the full warp.
+//   * Rows are distributed grid-stride over a persistent grid, U rows per thread and step (U = 4
+//     for narrow widths so that enough loads are in flight to stream at HBM speed); all lanes of
+//     a warp run the same trip count so the __syncwarp() is always reached by the full warp.
 #pragma once
 #include "common.cuh"
 #include "tsmttsm.cuh"  // tzero
@@ -37,7 +38,7 @@ struct TsmmArgs {
 
 constexpr int TSMM_THREADS = 256;
 
-template <typename T, typename Acc, int TN>
+template <typename T, typename Acc, int TN, int U>
 __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p) {
   typedef Ops<T, Acc> O;
   constexpr int NT = TSMM_THREADS;
@@ -50,32 +51,49 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
   }
   __syncthreads();
 
-  const int RS = NT / gn;  // rows per CTA step (gn divides 32, so NT % gn == 0)
+  // U rows per thread and step (r = base + j*RS + rs): for narrow products the loads of U rows
+  // are in flight together, which a streaming (HBM-bound) width needs
+  const int RS = NT / gn;  // rows per CTA step and unit (gn divides 32, so NT % gn == 0)
   const int cell = threadIdx.x % gn, rs = threadIdx.x / gn;
   const int n0 = cell * TN;
-  for (int64_t base = (int64_t)blockIdx.x * RS; base < p.K; base += (int64_t)gridDim.x * RS) {
-    const int64_t r = base + rs;
-    const bool valid = r < p.K;
-    Acc acc[TN];
+  const int64_t step = (int64_t)gridDim.x * RS * U;
+  for (int64_t base = (int64_t)blockIdx.x * RS * U; base < p.K; base += step) {
+    bool valid[U];
 #pragma unroll
-    for (int u = 0; u < TN; u++) acc[u] = O::zero();
-    if (valid) {
-      const T* a_row = p.A + r * p.lda;
+    for (int j = 0; j < U; j++) valid[j] = base + (int64_t)j * RS + rs < p.K;
+    Acc acc[U][TN];
+#pragma unroll
+    for (int j = 0; j < U; j++)
+#pragma unroll
+      for (int u = 0; u < TN; u++) acc[j][u] = O::zero();
 #pragma unroll 4
-      for (int m = 0; m < M; m++) {
-        const T a = a_row[m];
-        const T* b = Bs + m * np + n0;
+    for (int m = 0; m < M; m++) {
+      T a[U];
 #pragma unroll
-        for (int u = 0; u < TN; u++) acc[u] = O::mac(acc[u], a, b[u]);
-      }
+      for (int j = 0; j < U; j++) a[j] = valid[j] ? p.A[(base + (int64_t)j * RS + rs) * p.lda + m] : tzero<T>();
+      const T* b = Bs + m * np + n0;
+#pragma unroll
+      for (int j = 0; j < U; j++)
+#pragma unroll
+        for (int u = 0; u < TN; u++) acc[j][u] = O::mac(acc[j][u], a[j], b[u]);
     }
-    __syncwarp();  // the whole row has been read before any of it is overwritten (in place)
-    if (valid) {
-      T* c_row = p.C + r * p.ldc;
+    __syncwarp();  // the whole rows have been read before any of them is overwritten (in place)
+    T cv[U][TN];
+    if (!p.beta_zero) {  // C values of all U rows in flight together
+#pragma unroll
+      for (int j = 0; j < U; j++)
+#pragma unroll
+        for (int u = 0; u < TN; u++)
+          cv[j][u] = (valid[j] && n0 + u < N) ? p.C[(base + (int64_t)j * RS + rs) * p.ldc + n0 + u] : tzero<T>();
+    }
+#pragma unroll
+    for (int j = 0; j < U; j++) {
+      if (!valid[j]) continue;
+      T* c_row = p.C + (base + (int64_t)j * RS + rs) * p.ldc;
 #pragma unroll
       for (int u = 0; u < TN; u++) {
         const int n = n0 + u;
-        if (n < N) c_row[n] = O::finish(acc[u], p.alpha, p.beta, p.beta_zero != 0, c_row + n);
+        if (n < N) c_row[n] = O::finish(acc[j][u], p.alpha, p.beta, p.beta_zero != 0, &cv[j][u]);
       }
     }
   }
