@@ -243,9 +243,13 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
         return run_t<c32, c32>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
     case SKINNY_C64:
-      if (tsmm && (acc == SKINNY_ACC_SPLIT || (acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_NATIVE))) {
-        skinny_status s = split_tsmm(h, true, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
-                                     (double*)C, ldc, st, acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_SPLIT);
+      if (acc == SKINNY_ACC_SPLIT || (acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_NATIVE)) {
+        const bool autosel = acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_SPLIT;
+        skinny_status s =
+            tsmm ? split_tsmm(h, true, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+                              (double*)C, ldc, st, autosel)
+                 : split_complex_tsmttsm(h, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+                                         (double*)C, ldc, st, autosel);
         if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
       }
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)

@@ -549,11 +549,6 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   const int64_t RSW = (int64_t)sw * W;
   const bool aligned = ((uintptr_t)A % 16 == 0) && (a.gram || (uintptr_t)B % 16 == 0);
   const bool dense = lda <= 2 * M + 16 && (a.gram || ldb <= 2 * N + 16);
-  a.bulk = aligned && dense && K > RSW;
-  a.lda_s = a.bulk ? lda : M;
-  a.ldb_s = a.gram ? a.lda_s : (a.bulk ? ldb : N);
-  a.tile_a = (uint32_t)round_up(RSW * a.lda_s * 8, 128);
-  a.tile_b = a.gram ? 0u : (uint32_t)round_up(RSW * a.ldb_s * 8, 128);
   a.nmma = std::max(16, 8 * NP);
   a.tmem_cols = a.nmma <= 32 ? 32 : (a.nmma <= 64 ? 64 : 128);
   a.lbo_a = (uint32_t)(8 * a.MP * 16);
@@ -562,13 +557,25 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.dig_a = (uint32_t)round_up(octs * a.lbo_a + DPAD, 1024);
   a.dig_b = a.gram ? 0u : (uint32_t)round_up(octs * a.lbo_b, 1024);
   const int64_t dig = (int64_t)2 * (a.dig_a + a.dig_b);
-  const int64_t stage = round_up(a.tile_a + a.tile_b, 1024);
+  const int64_t fixed = HDR + SBYTES + dig;
+  // FP64 stages: whole (padded) rows by bulk copy where they fit two stages, else the M (N) used
+  // columns by plain loads
+  int64_t stage = 0;
+  int stages = 0;
+  for (int bulk = (aligned && dense && K > RSW) ? 1 : 0; bulk >= 0; bulk--) {
+    a.bulk = bulk;
+    a.lda_s = a.bulk ? lda : M;
+    a.ldb_s = a.gram ? a.lda_s : (a.bulk ? ldb : N);
+    a.tile_a = (uint32_t)round_up(RSW * a.lda_s * 8, 128);
+    a.tile_b = a.gram ? 0u : (uint32_t)round_up(RSW * a.ldb_s * 8, 128);
+    stage = round_up(a.tile_a + a.tile_b, 1024);
+    stages = (int)std::min<int64_t>(4, (h->dev.smem_optin - fixed) / stage);
+    if (stages >= 2) break;
+  }
   if (a.gram)
     a.tile_a = (uint32_t)stage;
   else
     a.tile_b = (uint32_t)(stage - a.tile_a);
-  const int64_t fixed = HDR + SBYTES + dig;
-  int stages = (int)std::min<int64_t>(4, (h->dev.smem_optin - fixed) / stage);
   if (stages < 2) {
     set_error("split precision: tiles do not fit in shared memory");
     return SKINNY_UNSUPPORTED;
