@@ -415,8 +415,27 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   using namespace stsmm;
   const int64_t Mr = cplx ? 2 * M : M, Nr = cplx ? 2 * N : N;
   if (Mr > 64 || Nr > 64) {
-    set_error("split precision TSMM: real widths M, N <= 64 in this build");
-    return SKINNY_UNSUPPORTED;
+    // wider products out of place run as passes of real width <= 64: output columns are
+    // independent, and the contraction accumulates through beta (the first pass applies beta,
+    // later passes add with beta = 1; each pass rounds once more in FP64)
+    const int64_t cw = cplx ? 32 : 64, w = cplx ? 2 : 1;
+    if (Mr > 128 || Nr > 128 || (const void*)A == (const void*)C) {
+      set_error("split precision TSMM: real widths <= 64, or <= 128 out of place");
+      return SKINNY_UNSUPPORTED;
+    }
+    if (autoselect && (K < 8192 || !(cplx ? M * N >= 64 : (M >= 16 && N >= 16)))) {
+      set_error("split precision TSMM: not selected automatically for this shape");
+      return SKINNY_UNSUPPORTED;
+    }
+    const double one[2] = {1.0, 0.0};
+    for (int64_t n0 = 0; n0 < N; n0 += cw)
+      for (int64_t m0 = 0; m0 < M; m0 += cw) {
+        const skinny_status s = split_tsmm(h, cplx, std::min(cw, M - m0), std::min(cw, N - n0), K, A + w * m0, lda,
+                                           alpha, B + w * (n0 * ldb + m0), ldb, m0 == 0 ? beta : (const void*)one,
+                                           C + w * n0, ldc, st, false);
+        if (s != SKINNY_OK) return s;
+      }
+    return SKINNY_OK;
   }
   // auto selection (measured on GB300, K with A of 1 GiB): FP64 split wins when both widths are
   // >= 16 (1.07x at 16x16 .. 5x at 64x64); complex FP64 from M*N >= 64 (1.16x at 4x16, 5.2x at

@@ -122,3 +122,34 @@ def test_split_tsmm_small_k(handle):
         handle.tsmm(M, N, K, dev(A), M, 1.0, dev(B), M, 0.0, Cd, N, acc="split")
         exp, den = common.tsmm_expected(M, N, K, A, M, B, M, np.zeros(K * N), N, 1.0, 0.0)
         assert common.normwise(host(Cd), exp, den) <= 8e-16, K
+
+
+@pytest.mark.parametrize("cplx,M,N", [(True, 64, 64), (True, 32, 64), (True, 64, 16), (True, 40, 33),
+                                      (False, 128, 128), (False, 96, 64), (False, 70, 20), (False, 16, 100)])
+def test_split_tsmm_wide_in_passes(handle, cplx, M, N):
+    """Real widths above 64 run as passes (output-column chunks; contraction chunks accumulate
+    through beta)."""
+    rng = np.random.default_rng(M * 7 + N + cplx)
+    K = 6007
+    dt = np.complex128 if cplx else np.float64
+    lda, ldb, ldc = M + 1, M, N + 2
+    A = common.uniform(rng, K * lda, dt)
+    B = common.uniform(rng, N * ldb, dt)
+    C0 = common.uniform(rng, K * ldc, dt)
+    alpha, beta = (0.5 + 0.25j, -0.75 + 0.5j) if cplx else (1.25, -0.5)
+    Cd = dev(C0)
+    handle.tsmm(M, N, K, dev(A), lda, alpha, dev(B), ldb, beta, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, A, lda, B, ldb, C0, ldc, alpha, beta)
+    err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
+    assert err <= min(common.tol(dt, M), 8e-16), err
+
+
+def test_split_tsmm_wide_in_place_unsupported(handle):
+    from skinny_matmul_gb300 import lib as L
+    M = 40
+    K = 1000
+    X = dev(np.zeros(K * M, np.complex128))
+    B = dev(np.zeros(M * M, np.complex128))
+    with pytest.raises(L.SkinnyError):
+        handle.tsmm(M, M, K, X, M, 1.0, B, M, 0.0, X, M, acc="split")
