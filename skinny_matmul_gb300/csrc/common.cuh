@@ -73,8 +73,11 @@ struct Ops<R, R> {  // float / double
   static __device__ __forceinline__ R mac(R acc, R a, R b) { return fma(a, b, acc); }
   static __device__ __forceinline__ R add(R x, R y) { return x + y; }
   static __device__ __forceinline__ bool is_zero(R v) { return v == R(0); }
+  // alpha == 1 skips the multiply (the same value: s * 1 == s); narrow TSMMs are bound by these
+  // epilogue operations on the FP64 pipe
   static __device__ __forceinline__ R finish(R s, R alpha, R beta, bool beta_zero, const R* c) {
-    return beta_zero ? alpha * s : (*c) * beta + s * alpha;
+    const R as = alpha == R(1) ? s : s * alpha;
+    return beta_zero ? as : fma(*c, beta, as);
   }
   static __device__ __forceinline__ R shfl_xor(R v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 };
@@ -93,7 +96,7 @@ struct Ops<cplx<R>, cplx<R>> {
   static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
   static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
   static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
-    C r = mul(alpha, s);
+    C r = (alpha.x == R(1) && alpha.y == R(0)) ? s : mul(alpha, s);
     if (!beta_zero) r = add(mul(beta, *c), r);
     return r;
   }
