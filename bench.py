@@ -359,6 +359,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload: skip the compact split-vs-FP64 and serving measurements")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve-c5: Poisson arrival rate per second")
+    ap.add_argument("--streams", type=int, default=8, help="serve-c5: request-loop streams")
+    ap.add_argument("--inflight", type=int, default=16, help="serve-c5: requests in flight at most")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -575,7 +577,7 @@ def c5_call(h, r, ops, stream=None):
         h.tsmm(r["M"], r["N"], r["K"], A, r["M"], 1.0, B, r["M"], 0.0, C, r["N"], acc=acc, stream=stream, dtype=dt)
 
 
-def serve_measure(h, dev, n, rate, rank):
+def serve_measure(h, dev, n, rate, rank, streams=8, inflight=16):
     """Run the C5 stream both ways; returns (one-per-call stats, served stats, bytes, served wall)."""
     import numpy as np
     import torch
@@ -609,7 +611,7 @@ def serve_measure(h, dev, n, rate, rank):
         return time.perf_counter() - t0, lat
 
     def served():
-        srv = Server(h, 120 * (1 << 30), num_streams=8, max_inflight=16)
+        srv = Server(h, 120 * (1 << 30), num_streams=streams, max_inflight=inflight)
         tickets = []
         t0 = time.perf_counter()
         for i, (r, o) in enumerate(zip(reqs, ops)):
@@ -670,7 +672,7 @@ def run_serve(args):
     n = args.requests
     n0 = L.skinny_kernel_launches()
     with ClockSampler(local) as clk:
-        seq, srv, total_bytes, wall_srv = serve_measure(h, dev, n, args.rate, rank)
+        seq, srv, total_bytes, wall_srv = serve_measure(h, dev, n, args.rate, rank, args.streams, args.inflight)
     launches = L.skinny_kernel_launches() - n0
     h.check_device()
     value = sum_over_ranks(total_bytes / wall_srv / 1e9, world)
@@ -681,7 +683,7 @@ def run_serve(args):
                 "vs_baseline": None, "dtype": "mixed (f64 60%, c64 25%, f32 15%)",
                 "data": "synthetic U[-1,1) operands resident in HBM, seeded; Poisson arrivals",
                 "config": {"workload": "serve-c5", "description": WORKLOADS["serve-c5"][1], "requests": n,
-                           "arrival_rate_per_s": args.rate, "l2": "operands larger than L2 for most requests",
+                           "arrival_rate_per_s": args.rate, "streams": args.streams, "max_inflight": args.inflight, "l2": "operands larger than L2 for most requests",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "roofline": {"bound": "hbm", "achieved": round(value, 1), "peak": hbm, "unit": "GB/s",
                              "frac": round(value / hbm, 4), "traffic": None, "kernel": "request mix"},

@@ -15,8 +15,8 @@
 //     product of the last (L-1) planes of A' with the first (L-1) planes of B' pairs exactly the
 //     digits with i + j = L, so one MMA chain per level gives D_L(r, n) = sum_{i+j=L} sum_m a_i b_j.
 //   * |D_L| <= 8 * MP * 2^14 <= 2^23: exact in the FP32 TMEM accumulator.
-//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers, its top 64 bits (from its
-//     own leading bit; the rest lies below 2^-62 of |V|) are rounded to a double with integer
+//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers, its top 61+ bits (from its
+//     own leading bit; the rest lies below 2^-61 of |V|) are rounded to a double with integer
 //     instructions and scaled by 2^(e_r + f_n - 2112) in the exponent field; beta*C is one FMA.
 //     Levels >= 10 are dropped (weight below 2^-56 of the leading level).
 //   * Tiles of 128 rows: two threads per row read the row's FP64 values straight from global
@@ -265,11 +265,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
           // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
           const long long H = ((long long)dl[0] * 256 + dl[1]) * 65536 + ((long long)dl[2] * 256 + dl[3]);
           const long long Lo = ((long long)dl[4] * 256 + dl[5]) * 65536 + ((long long)dl[6] * 256 + dl[7]);
-          // the top 64 bits of V starting at its own leading bit: shift H up by k = clz(|H|) - 1
-          // (k = 32: V fits in 64 bits and is kept whole); the bits of Lo dropped lie below 2^-62
-          // of |V|
+          // the top bits of V from its own leading bit: shift H up by k = clz(|H|) - 2, so that
+          // |H << k| < 2^62 and adding the |Lo| part (< 2^48) cannot pass 2^63 (k = 32: V fits in
+          // 64 bits and is kept whole); at least 61 bits are kept, the bits of Lo dropped lie below
+          // 2^-61 of |V|
           const long long aH = H < 0 ? -H : H;
-          const int k = aH ? min(32, __clzll(aH) - 1) : 32;
+          const int k = aH ? min(32, __clzll(aH) - 2) : 32;
           const long long top = (H << k) + (Lo >> (32 - k));
           double v = i64_to_double(top, e + fcol[n] - 2112 + 32 - k);
           if (!p.beta_zero) {

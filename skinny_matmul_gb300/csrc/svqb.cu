@@ -4,8 +4,9 @@
 // (the reference copies S to the host and calls MAGMA's dsyevd there, svqb.cu:95-120):
 //   1. S = X^T X                      TSMTTSM in Gram mode, method chosen by the caller
 //   2. d_i = 1/sqrt(S_ii) if |S_ii| > 1e-15 else 0;  S <- D S D        (svqb.cu:99-110)
-//   3. S = U L U^T                    one-CTA cyclic Jacobi in FP64 (parallel round-robin order),
-//                                     eigenvalues ascending as dsyevd returns them
+//   3. S = U L U^T                    one-CTA cyclic Jacobi in FP64 (parallel round-robin order:
+//                                     the M/2 rotations of a round at once), eigenvalues
+//                                     ascending as dsyevd returns them
 //   4. T = D U diag(1/sqrt(max(1e-15, l)))  stored as TSMM's B (B[n*M+m])  (svqb.cu:115-119)
 //   5. X <- X T                       in-place TSMM                      (svqb.cu:124-129)
 //   6. optional ||Q^T Q - I||_F with a double-double Gram                (svqb.cu:184-211)
@@ -33,7 +34,11 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_eig_kernel(const double* __
   double* cs = d + M;             // 2 * (M/2 + 1)
   double* red = cs + 2 * (M / 2 + 1);  // SVQB_THREADS
   int* order = reinterpret_cast<int*>(red + SVQB_THREADS);  // M
+  int* pq = order + SVQB_MAX_M;                             // 2 * (M/2 + 1): the round's pairs
   const int tid = threadIdx.x;
+  // rotation work: thread = (pair lane k0, row / column i0); no division by runtime values
+  constexpr int KS = SVQB_THREADS / SVQB_MAX_M;
+  const int i0 = tid % SVQB_MAX_M, k0 = tid / SVQB_MAX_M;
 
   for (int i = tid; i < M; i += SVQB_THREADS) {
     double sii = S[i * M + i];
@@ -49,6 +54,10 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_eig_kernel(const double* __
 
   const int n = (M + 1) & ~1;  // players of the round-robin (a dummy when M is odd)
   const int npairs = n / 2;
+  // converged when the off-diagonal mass is at the rounding level of the matrix ((M u)^2 of the
+  // whole), or when it is small and a sweep no longer reduces it (rounding noise)
+  const double tol = (double)M * M * 1.23e-32;
+  double prev_off = 0.0;
   int sweeps = 0;
   for (; sweeps < max_sweeps; sweeps++) {
     // convergence: off-diagonal mass relative to the whole matrix
@@ -75,10 +84,13 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_eig_kernel(const double* __
     }
     const double all_sum = red[0];
     __syncthreads();
-    if (off_sum <= 1.0e-32 * all_sum || M == 1) break;
+    if (off_sum <= tol * all_sum || M == 1 || (sweeps > 0 && off_sum <= 1.0e-20 * all_sum && off_sum >= 0.25 * prev_off))
+      break;
+    prev_off = off_sum;
 
     for (int r = 0; r < n - 1; r++) {
-      // pair k: (n-1, r) for k = 0, ((r+k) % (n-1), (r-k+n-1) % (n-1)) otherwise
+      // pair k: (n-1, r) for k = 0, ((r+k) % (n-1), (r-k+n-1) % (n-1)) otherwise; the rotation
+      // of each pair and the pair itself go to shared memory once per round
       for (int k = tid; k < npairs; k += SVQB_THREADS) {
         int p = k == 0 ? n - 1 : (r + k) % (n - 1);
         int q = k == 0 ? r : (r - k + n - 1) % (n - 1);
@@ -96,47 +108,39 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_eig_kernel(const double* __
             c = 1.0 / sqrt(1.0 + t * t);
             s = t * c;
           }
+        } else {
+          q = p;  // the dummy player: an identity rotation on p
         }
         cs[2 * k] = c;
         cs[2 * k + 1] = s;
+        pq[2 * k] = p;
+        pq[2 * k + 1] = q;
       }
       __syncthreads();
-      // A <- A J, V <- V J (column rotations): item (k, i)
-      for (int e = tid; e < npairs * M; e += SVQB_THREADS) {
-        int k = e / M, i = e % M;
-        int p = k == 0 ? n - 1 : (r + k) % (n - 1);
-        int q = k == 0 ? r : (r - k + n - 1) % (n - 1);
-        if (p > q) {
-          int x = p;
-          p = q;
-          q = x;
+      // A <- A J, V <- V J (column rotations): thread (k0, i) takes row i of pairs k0, k0 + KS, ...
+      if (i0 < M)
+        for (int k = k0; k < npairs; k += KS) {
+          const int p = pq[2 * k], q = pq[2 * k + 1];
+          if (p == q) continue;
+          const double c = cs[2 * k], s = cs[2 * k + 1];
+          const double aip = A[i0 * LD + p], aiq = A[i0 * LD + q];
+          A[i0 * LD + p] = c * aip - s * aiq;
+          A[i0 * LD + q] = s * aip + c * aiq;
+          const double vip = V[i0 * LD + p], viq = V[i0 * LD + q];
+          V[i0 * LD + p] = c * vip - s * viq;
+          V[i0 * LD + q] = s * vip + c * viq;
         }
-        if (q >= M) continue;
-        const double c = cs[2 * k], s = cs[2 * k + 1];
-        double aip = A[i * LD + p], aiq = A[i * LD + q];
-        A[i * LD + p] = c * aip - s * aiq;
-        A[i * LD + q] = s * aip + c * aiq;
-        double vip = V[i * LD + p], viq = V[i * LD + q];
-        V[i * LD + p] = c * vip - s * viq;
-        V[i * LD + q] = s * vip + c * viq;
-      }
       __syncthreads();
-      // A <- J^T A (row rotations): item (k, j)
-      for (int e = tid; e < npairs * M; e += SVQB_THREADS) {
-        int k = e / M, j = e % M;
-        int p = k == 0 ? n - 1 : (r + k) % (n - 1);
-        int q = k == 0 ? r : (r - k + n - 1) % (n - 1);
-        if (p > q) {
-          int x = p;
-          p = q;
-          q = x;
+      // A <- J^T A (row rotations): thread (k0, j) takes column j
+      if (i0 < M)
+        for (int k = k0; k < npairs; k += KS) {
+          const int p = pq[2 * k], q = pq[2 * k + 1];
+          if (p == q) continue;
+          const double c = cs[2 * k], s = cs[2 * k + 1];
+          const double apj = A[p * LD + i0], aqj = A[q * LD + i0];
+          A[p * LD + i0] = c * apj - s * aqj;
+          A[q * LD + i0] = s * apj + c * aqj;
         }
-        if (q >= M) continue;
-        const double c = cs[2 * k], s = cs[2 * k + 1];
-        double apj = A[p * LD + j], aqj = A[q * LD + j];
-        A[p * LD + j] = c * apj - s * aqj;
-        A[q * LD + j] = s * apj + c * aqj;
-      }
       __syncthreads();
     }
   }
@@ -189,7 +193,8 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_orth_kernel(const double* _
 }
 
 static size_t svqb_eig_smem(int M) {
-  return (size_t)(2 * M * (M + 1) + M + 2 * (M / 2 + 1) + SVQB_THREADS) * sizeof(double) + M * sizeof(int) + 64;
+  return (size_t)(2 * M * (M + 1) + M + 2 * (M / 2 + 1) + SVQB_THREADS) * sizeof(double) +
+         (SVQB_MAX_M + 2 * (M / 2 + 1)) * sizeof(int) + 64;
 }
 
 }  // namespace skinny

@@ -153,3 +153,33 @@ def test_split_tsmm_wide_in_place_unsupported(handle):
     B = dev(np.zeros(M * M, np.complex128))
     with pytest.raises(L.SkinnyError):
         handle.tsmm(M, M, K, X, M, 1.0, B, M, 0.0, X, M, acc="split")
+
+
+def test_split_tsmm_epilogue_window_no_overflow(handle):
+    """A row and column whose level-2..5 sum H lies just below 2^35 in magnitude while the
+    lower levels add in the same direction: shifting H up to bit 62 and adding the low part
+    overflowed int64 once (the SVQB transform of a Gaussian block hit it).  Exact value from the
+    oracle."""
+    a = np.array([-0.0902333034774286, 0.9953960347960409, -2.0001290059485535, 1.1617594199348404,
+                  0.028492030066136674, 0.09951610977610051, -0.5629304941495062, -0.5286079153781488,
+                  -0.06524758134155434, 2.6990741536801366, -1.2709225246596088, 0.7713573735580164,
+                  -0.6003361654324079, 1.3004598145928816, -1.444973049978174, -0.6231094244429115])
+    b = np.array([-0.00011886051243768427, 3.243606984224829e-05, -0.00021251367167326099,
+                  -0.0003335254616945151, -0.000156368179871508, 4.834772800842875e-06,
+                  -0.0004869401572375484, 0.00041763952392900086, 7.545508081615978e-05,
+                  -0.0001768818370975454, 0.00024901494173812844, -0.00036403177288671997,
+                  -0.00016018322106158998, -2.026052523593613e-05, -5.568237286745128e-05,
+                  0.00028435164789257793])
+    M, N = 16, 16
+    K = 300
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((K, M))
+    A[137] = a
+    B = rng.standard_normal((N, M)) * 1e-4
+    B[13] = b
+    Cd = dev(np.zeros(K * N))
+    handle.tsmm(M, N, K, dev(A.ravel()), M, 1.0, dev(B.ravel()), M, 0.0, Cd, N, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, A.ravel(), M, B.ravel(), M, np.zeros(K * N), N, 1.0, 0.0)
+    assert common.normwise(got, exp, den) <= 8e-16
+    assert abs(got[137 * N + 13] - exp[137 * N + 13]) <= 2e-16 * abs(exp[137 * N + 13])
