@@ -99,6 +99,14 @@ skinny_status skinny_tsmm(skinny_handle handle, skinny_dtype dtype, skinny_acc a
                           int64_t N, int64_t K, const void* A, int64_t lda, const void* alpha,
                           const void* B, int64_t ldb, const void* beta, void* C, int64_t ldc,
                           void* stream);
+/* C = alpha A^H B + beta C: the conjugate transpose of A (Hermitian Gram when A == B).  No
+ * counterpart in the reference, whose complex TSMTTSM uses the plain transpose (cuBLAS OP_T,
+ * tsmttsm/gen_cublas.cuh:29-39); complex orthogonalisation needs this form.  Same arguments as
+ * skinny_tsmttsm; for real dtypes identical to it.  Methods: native, auto, split (complex FP64,
+ * M, N <= 64). */
+skinny_status skinny_tsmttsm_conj(skinny_handle handle, skinny_dtype dtype, skinny_acc acc, int64_t M, int64_t N,
+                                  int64_t K, const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                                  const void* beta, void* C, int64_t ldc, void* stream);
 
 /* SVQB orthogonalisation of X (K x M row-major, ldx >= M, FP64), in place, entirely on the
  * device; replaces svqb/svqb.cu:72-130 (which runs the eigensolve on the host through MAGMA).
@@ -109,6 +117,14 @@ skinny_status skinny_tsmm(skinny_handle handle, skinny_dtype dtype, skinny_acc a
  * and written there after a stream synchronisation (svqb/svqb.cu:184-211 getL2Error). */
 skinny_status skinny_svqb(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M,
                           double* X, int64_t ldx, double* orth_err_out, void* stream);
+
+/* CholQR (passes = 1) / CholQR2 (passes = 2) of X (K x M, FP64, M <= 64) in place: per pass the
+ * Gram S = X^T X (method gram_acc), the Cholesky S = R^T R and X <- X R^-1 by the in-place TSMM,
+ * all on the device.  No counterpart in the reference (its orthogonalisation is SVQB); the same
+ * building blocks.  SKINNY_BAD_ARG when a Gram is not numerically positive definite.
+ * orth_err_out (nullable): ||Q^T Q - I||_F with a double-double Gram (synchronises the stream). */
+skinny_status skinny_cholqr(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M, double* X, int64_t ldx,
+                            int passes, double* orth_err_out, void* stream);
 
 /* FP64 TSMTTSM that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: code that runs under an allocator owning the whole

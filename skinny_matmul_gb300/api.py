@@ -82,10 +82,12 @@ class Handle:
                 ctypes.byref(be), _ptr(C), ldc, _stream(stream))
         return L.check(st)
 
-    def tsmttsm(self, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, dtype=None):
-        """C[n*ldc+m] = alpha * sum_k A[k*lda+m] B[k*ldb+n] + beta * C[n*ldc+m]."""
-        return self._product(self.lib.skinny_tsmttsm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc,
-                             acc, stream, dtype)
+    def tsmttsm(self, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, dtype=None,
+                conj=False):
+        """C[n*ldc+m] = alpha * sum_k A[k*lda+m] B[k*ldb+n] + beta * C[n*ldc+m]; conj=True takes the
+        conjugate of A (C = alpha A^H B + beta C)."""
+        fn = self.lib.skinny_tsmttsm_conj if conj else self.lib.skinny_tsmttsm
+        return self._product(fn, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc, stream, dtype)
 
     def tsmm(self, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None, dtype=None):
         """C[r*ldc+n] = alpha * sum_m A[r*lda+m] B[n*ldb+m] + beta * C[r*ldc+n]  (A may be C)."""
@@ -109,6 +111,14 @@ class Handle:
 
     def tune_import(self, text: str):
         return L.check(self.lib.skinny_tune_import(self.h, text.encode()))
+
+    def cholqr(self, K, M, X, ldx, passes=2, gram_acc="auto", orth_err=True, stream=None):
+        """In-place CholQR (passes=1) / CholQR2 (passes=2) of X (K x M, FP64); returns
+        ||Q^T Q - I||_F when orth_err."""
+        err = ctypes.c_double(-1.0)
+        L.check(self.lib.skinny_cholqr(self.h, _ACC[gram_acc], K, M, _ptr(X), ldx, passes,
+                                       ctypes.byref(err) if orth_err else None, _stream(stream)))
+        return err.value if orth_err else None
 
     def svqb(self, K, M, X, ldx, gram_acc="split", orth_err=True, stream=None):
         """In-place SVQB of X (K x M, FP64); returns ||Q^T Q - I||_F when orth_err."""

@@ -75,7 +75,8 @@ skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const
 // (split_complex.cu); M, N <= 64.
 skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64_t K, const double* A,
                                     int64_t lda, const void* alpha, const double* B, int64_t ldb,
-                                    const void* beta, double* C, int64_t ldc, cudaStream_t st, bool autoselect);
+                                    const void* beta, double* C, int64_t ldc, cudaStream_t st, bool autoselect,
+                                    bool conj = false);
 
 // FP64 / complex FP64 TSMM in split precision (split_tsmm.cu); SKINNY_UNSUPPORTED outside its range.
 skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64_t K, const double* A,

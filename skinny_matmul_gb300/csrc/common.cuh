@@ -22,6 +22,13 @@ struct __align__(2 * sizeof(R)) cplx {
 };
 typedef cplx<float> c32;
 typedef cplx<double> c64;
+// the same storage, marking a TSMTTSM whose left operand is conjugated: C = alpha A^H B + beta C
+template <typename R>
+struct __align__(2 * sizeof(R)) cplxh {
+  R x, y;
+};
+typedef cplxh<float> c32h;
+typedef cplxh<double> c64h;
 
 // ---------------------------------------------------------------- double-double primitives
 __device__ __forceinline__ dd dd_fast2sum(double a, double b) {
@@ -91,6 +98,29 @@ struct Ops<cplx<R>, cplx<R>> {
     acc.x = fma(-a.y, b.y, acc.x);
     acc.y = fma(a.x, b.y, acc.y);
     acc.y = fma(a.y, b.x, acc.y);
+    return acc;
+  }
+  static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
+  static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+  static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
+    C r = (alpha.x == R(1) && alpha.y == R(0)) ? s : mul(alpha, s);
+    if (!beta_zero) r = add(mul(beta, *c), r);
+    return r;
+  }
+  static __device__ __forceinline__ C shfl_xor(C v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
+  }
+};
+
+template <typename R>
+struct Ops<cplxh<R>, cplxh<R>> {  // conj(a) * b per term (A^H B)
+  typedef cplxh<R> C;
+  static __device__ __forceinline__ C zero() { return {R(0), R(0)}; }
+  static __device__ __forceinline__ C mac(C acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
     return acc;
   }
   static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }

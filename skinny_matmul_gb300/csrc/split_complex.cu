@@ -5,7 +5,8 @@
 // re, im, re, im, ...).  Their real product P = A_r^T B_r (2M x 2N, split precision: split.cu
 // for 2M, 2N <= 16, split_wide.cu up to 128) holds all four real products:
 //   P[2n][2m] = ArT Br,  P[2n+1][2m+1] = AiT Bi,  P[2n+1][2m] = ArT Bi,  P[2n][2m+1] = AiT Br
-// and C = alpha (P_rr - P_ii + i (P_ri + P_ir)) + beta C (plain transpose, as the reference).
+// and C = alpha (P_rr - P_ii + i (P_ri + P_ir)) + beta C (plain transpose, as the reference), or
+// alpha (P_rr + P_ii + i (P_ri - P_ir)) + beta C for the conjugate transpose A^H B.
 // Each P entry carries the split kernels' accuracy; the combination adds FP64 roundings only.
 #include <cstring>
 
@@ -18,13 +19,14 @@ namespace {
 constexpr int CMAX = 64;  // complex widths (real 128)
 
 __global__ void combine_kernel(const double* __restrict__ P, int ldp, int M, int N, double ar, double ai, double br,
-                               double bi, int beta_zero, double* __restrict__ C, int64_t ldc) {
+                               double bi, int beta_zero, int conj, double* __restrict__ C, int64_t ldc) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= M * N) return;
   const int m = e % M, n = e / M;
   const double rr = P[(2 * n) * ldp + 2 * m], ii = P[(2 * n + 1) * ldp + 2 * m + 1];
   const double ri = P[(2 * n + 1) * ldp + 2 * m], ir = P[(2 * n) * ldp + 2 * m + 1];
-  const double sr = rr - ii, si = ri + ir;
+  // A^T B: (rr - ii, ri + ir); A^H B (conjugated A): (rr + ii, ri - ir)
+  const double sr = conj ? rr + ii : rr - ii, si = conj ? ri - ir : ri + ir;
   double vr = ar * sr - ai * si, vi = ar * si + ai * sr;
   double* c = C + 2 * ((int64_t)n * ldc + m);
   if (!beta_zero) {
@@ -40,7 +42,8 @@ __global__ void combine_kernel(const double* __restrict__ P, int ldp, int M, int
 
 skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64_t K, const double* A,
                                     int64_t lda, const void* alpha, const double* B, int64_t ldb,
-                                    const void* beta, double* C, int64_t ldc, cudaStream_t st, bool autoselect) {
+                                    const void* beta, double* C, int64_t ldc, cudaStream_t st, bool autoselect,
+                                    bool conj) {
   if (M > CMAX || N > CMAX) {
     set_error("split precision complex TSMTTSM: M, N <= 64");
     return SKINNY_UNSUPPORTED;
@@ -66,7 +69,7 @@ skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64
   std::memcpy(be, beta, sizeof be);
   const int cells = (int)(M * N);
   combine_kernel<<<(cells + 255) / 256, 256, 0, st>>>(P, (int)(2 * M), (int)M, (int)N, al[0], al[1], be[0], be[1],
-                                                      be[0] == 0.0 && be[1] == 0.0, C, ldc);
+                                                      be[0] == 0.0 && be[1] == 0.0, conj ? 1 : 0, C, ldc);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <string>
 
 #include "api_internal.h"
 
@@ -192,6 +193,60 @@ __global__ void __launch_bounds__(SVQB_THREADS) svqb_orth_kernel(const double* _
   if (threadIdx.x == 0) *out = sqrt(red[0]);
 }
 
+// Cholesky S = R^T R (R upper, positive diagonal) of the Gram matrix and T = R^-1 in TSMM's B
+// layout (B[n*M + m] = Rinv[m][n]), so that X <- X T gives Q = X R^-1.  *info = 0, or j + 1 when
+// the pivot of column j is not positive (the Gram is not numerically positive definite).
+__global__ void __launch_bounds__(SVQB_THREADS) cholqr_kernel(const double* __restrict__ S, int M,
+                                                              double* __restrict__ T, int* info) {
+  extern __shared__ __align__(16) double sh[];
+  const int LD = M + 1;
+  double* A = sh;         // M x LD: the trailing matrix, then R in the upper triangle
+  double* Y = A + M * LD;  // M x LD: R^-1
+  __shared__ int bad;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < M * M; e += SVQB_THREADS) A[(e / M) * LD + e % M] = S[e];
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < M; j++) {
+    const double piv = A[j * LD + j];
+    if (!(piv > 0.0)) {  // uniform: every thread reads the same pivot
+      if (tid == 0) bad = j + 1;
+      break;
+    }
+    const double r = sqrt(piv);
+    __syncthreads();
+    for (int i = j + 1 + tid; i < M; i += SVQB_THREADS) A[j * LD + i] /= r;  // row j of R
+    if (tid == 0) A[j * LD + j] = r;
+    __syncthreads();
+    // trailing update A[i][l] -= R[j][i] R[j][l] for j < i <= l
+    const int w = M - j - 1;
+    for (int e = tid; e < w * w; e += SVQB_THREADS) {
+      const int i = j + 1 + e / w, l = j + 1 + e % w;
+      if (l >= i) A[i * LD + l] -= A[j * LD + i] * A[j * LD + l];
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) *info = bad;
+    return;
+  }
+  // R^-1 column by column (back substitution), one thread per column
+  for (int c = tid; c < M; c += SVQB_THREADS) {
+    for (int i = M - 1; i >= 0; i--) {
+      double v = (i == c) ? 1.0 : 0.0;
+      for (int k = i + 1; k <= c; k++) v -= A[i * LD + k] * Y[k * LD + c];
+      Y[i * LD + c] = i > c ? 0.0 : v / A[i * LD + i];
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < M * M; e += SVQB_THREADS) {
+    const int n = e / M, m = e % M;
+    T[e] = Y[m * LD + n];
+  }
+  if (tid == 0) *info = 0;
+}
+
 static size_t svqb_eig_smem(int M) {
   return (size_t)(2 * M * (M + 1) + M + 2 * (M / 2 + 1) + SVQB_THREADS) * sizeof(double) +
          (SVQB_MAX_M + 2 * (M / 2 + 1)) * sizeof(int) + 64;
@@ -267,6 +322,90 @@ extern "C" skinny_status skinny_svqb(skinny_handle h, skinny_acc gram_acc, int64
         cudaStreamSynchronize(st) != cudaSuccess) {
       cudaGetLastError();
       set_error("svqb: reading the orthogonality error failed");
+      return SKINNY_DEVICE_ERROR;
+    }
+    *orth_err_out = v;
+  }
+  return SKINNY_OK;
+}
+
+// CholQR (passes = 1) / CholQR2 (passes = 2): Gram, Cholesky and in-place TSMM with R^-1 per pass.
+// No counterpart in the reference (whose orthogonalisation is SVQB, svqb/svqb.cu:72-130); it
+// reuses the same Gram and in-place TSMM.  SKINNY_BAD_ARG when a Gram is not numerically positive
+// definite (X is then left as the previous pass made it).
+extern "C" skinny_status skinny_cholqr(skinny_handle h, skinny_acc gram_acc, int64_t K, int64_t M, double* X,
+                                       int64_t ldx, int passes, double* orth_err_out, void* stream) {
+  set_error("");
+  if (!h) {
+    set_error("null handle");
+    return SKINNY_BAD_ARG;
+  }
+  if (M < 1 || K < 0 || ldx < M || (K > 0 && !X) || passes < 1 || passes > 4) {
+    set_error("cholqr: bad sizes, null X or passes outside 1..4");
+    return SKINNY_BAD_ARG;
+  }
+  if (M > SVQB_MAX_M) {
+    set_error("cholqr: M > 64 not provided");
+    return SKINNY_UNSUPPORTED;
+  }
+  DevGuard g(h->dev.id);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(h->mu);
+  const size_t need = (3 * (size_t)SVQB_MAX_M * SVQB_MAX_M + 8) * sizeof(double);
+  void*& buf = h->svqb_ws[st];
+  if (!buf) {
+    if (cudaMalloc(&buf, need) != cudaSuccess) {
+      cudaGetLastError();
+      buf = nullptr;
+      set_error("cholqr: cudaMalloc failed");
+      return SKINNY_NO_MEM;
+    }
+    h->extra_allocs.push_back(buf);
+  }
+  double* S = static_cast<double*>(buf);
+  double* T = S + SVQB_MAX_M * SVQB_MAX_M;
+  double* S2 = T + SVQB_MAX_M * SVQB_MAX_M;
+  double* errd = S2 + SVQB_MAX_M * SVQB_MAX_M;
+  int* info = reinterpret_cast<int*>(errd + 1);
+  const double one = 1.0, zero = 0.0;
+  LaunchOpts o{};
+  const size_t smem = (size_t)2 * M * (M + 1) * sizeof(double);
+  static std::atomic<int> attr{0};
+  ensure_smem_attr(cholqr_kernel, (int)smem, attr);
+  for (int pass = 0; pass < passes; pass++) {
+    skinny_status s = dispatch_product(h, false, SKINNY_R64, gram_acc, M, M, K, X, ldx, &one, X, ldx, &zero, S, M,
+                                       st, o);
+    if (s == SKINNY_UNSUPPORTED && gram_acc == SKINNY_ACC_SPLIT)
+      s = dispatch_product(h, false, SKINNY_R64, SKINNY_ACC_NATIVE, M, M, K, X, ldx, &one, X, ldx, &zero, S, M, st, o);
+    if (s != SKINNY_OK) return s;
+    cholqr_kernel<<<1, SVQB_THREADS, smem, st>>>(S, (int)M, T, info);
+    count_launch();
+    int hinfo = 0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cholqr: Cholesky launch failed");
+      return SKINNY_DEVICE_ERROR;
+    }
+    if (hinfo != 0) {
+      set_error("cholqr: Gram matrix not positive definite at column " + std::to_string(hinfo - 1));
+      return SKINNY_BAD_ARG;
+    }
+    s = dispatch_product(h, true, SKINNY_R64, SKINNY_ACC_AUTO, M, M, K, X, ldx, &one, T, M, &zero, X, ldx, st, o);
+    if (s != SKINNY_OK) return s;
+  }
+  if (orth_err_out) {
+    skinny_status s = dispatch_product(h, false, SKINNY_R64, SKINNY_ACC_DD, M, M, K, X, ldx, &one, X, ldx, &zero,
+                                       S2, M, st, o);
+    if (s != SKINNY_OK) return s;
+    svqb_orth_kernel<<<1, SVQB_THREADS, 0, st>>>(S2, (int)M, errd);
+    count_launch();
+    double v = -1.0;
+    if (cudaMemcpyAsync(&v, errd, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cholqr: reading the orthogonality error failed");
       return SKINNY_DEVICE_ERROR;
     }
     *orth_err_out = v;

@@ -54,6 +54,14 @@ template <>
 __device__ __forceinline__ c64 tzero<c64>() {
   return {0.0, 0.0};
 }
+template <>
+__device__ __forceinline__ c32h tzero<c32h>() {
+  return {0.f, 0.f};
+}
+template <>
+__device__ __forceinline__ c64h tzero<c64h>() {
+  return {0.0, 0.0};
+}
 
 // L2-coherent loads of partials written by other CTAs (L1 is not coherent across SMs).
 __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
@@ -63,6 +71,14 @@ __device__ __forceinline__ c32 ldcg(const c32* p) {
   return {v.x, v.y};
 }
 __device__ __forceinline__ c64 ldcg(const c64* p) {
+  double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return {v.x, v.y};
+}
+__device__ __forceinline__ c32h ldcg(const c32h* p) {
+  float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+__device__ __forceinline__ c64h ldcg(const c64h* p) {
   double2 v = __ldcg(reinterpret_cast<const double2*>(p));
   return {v.x, v.y};
 }

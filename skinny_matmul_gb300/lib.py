@@ -75,8 +75,10 @@ SIGNATURES = {
     "skinny_check_device": (_i, [_vp]),
     "skinny_kernel_launches": (ctypes.c_uint64, []),
     "skinny_tsmttsm": (_i, _PROD),
+    "skinny_tsmttsm_conj": (_i, _PROD),
     "skinny_tsmm": (_i, _PROD),
     "skinny_svqb": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "skinny_cholqr": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _i, _vp, _vp]),
     "skinny_autotune": (_i, [_vp, _i, _i, _i, _i64, _i64, _i64, _vp]),
     "skinny_tune_export": (_i, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)]),
     "skinny_tune_import": (_i, [_vp, ctypes.c_char_p]),

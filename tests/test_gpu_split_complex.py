@@ -78,3 +78,41 @@ def test_split_complex_too_wide_unsupported(handle):
     Cd = dev(np.zeros(M * N, np.complex128))
     with pytest.raises(L.SkinnyError):
         handle.tsmttsm(M, N, K, A, M, 1.0, B, N, 0.0, Cd, M, acc="split")
+
+
+@pytest.mark.parametrize("acc", ["native", "split", "auto"])
+@pytest.mark.parametrize("M,N,K", [(1, 1, 3000), (4, 4, 20000), (8, 3, 7001), (16, 16, 9000), (40, 24, 5000),
+                                   (64, 64, 4000)])
+def test_conjugate_transpose(handle, acc, M, N, K):
+    """C = alpha A^H B + beta C (skinny_tsmttsm_conj) against the oracle given conj(A)."""
+    rng = np.random.default_rng(M + 3 * N + K)
+    A = common.uniform(rng, K * M, np.complex128)
+    B = common.uniform(rng, K * N, np.complex128)
+    C0 = common.uniform(rng, N * M, np.complex128)
+    alpha, beta = 0.5 - 1.0j, -0.25 + 0.5j
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), M, alpha, dev(B), N, beta, Cd, M, acc=acc, conj=True)
+    exp, den = common.tsmttsm_expected(M, N, K, np.conj(A), M, B, N, C0, M, alpha, beta)
+    err = common.normwise(host(Cd), exp, den)
+    assert err <= common.tol(np.complex128, K), err
+    if acc == "split":
+        assert err <= 8e-16
+
+
+@pytest.mark.parametrize("dt", [np.complex64, np.complex128])
+def test_conjugate_gram_is_hermitian_and_real_dtypes_unchanged(handle, dt):
+    rng = np.random.default_rng(11)
+    M, K = 12, 30000
+    X = common.uniform(rng, K * M, dt)
+    Xd = dev(X)
+    Cd = dev(np.zeros(M * M, dt))
+    handle.tsmttsm(M, M, K, Xd, M, 1.0, Xd, M, 0.0, Cd, M, acc="native", conj=True)
+    G = host(Cd).reshape(M, M)
+    assert np.allclose(G, G.conj().T, rtol=0, atol=1e-4 if dt == np.complex64 else 1e-10)
+    assert np.all(np.diag(G).real > 0) and np.max(np.abs(np.diag(G).imag)) <= (1e-2 if dt == np.complex64 else 1e-9)
+    R = rng.uniform(-1, 1, K * M)
+    Rd = dev(R)
+    C1, C2 = dev(np.zeros(M * M)), dev(np.zeros(M * M))
+    handle.tsmttsm(M, M, K, Rd, M, 1.0, Rd, M, 0.0, C1, M, acc="native", conj=True)
+    handle.tsmttsm(M, M, K, Rd, M, 1.0, Rd, M, 0.0, C2, M, acc="native")
+    assert np.array_equal(host(C1), host(C2))
