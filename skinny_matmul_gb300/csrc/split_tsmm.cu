@@ -164,8 +164,10 @@ __device__ __forceinline__ double i64_to_double(long long x, int E) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
+// contraction width 16 (TMEM <= 256 columns, shared memory < 114 KB): two CTAs per SM, so that one
+// CTA's barriers overlap the other's work
 template <int MP>
-__global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
+__global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(const Args p) {
   constexpr int HALF = MP / 2;  // columns sliced per thread (two threads per row)
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bar_mma = reinterpret_cast<uint64_t*>(smem + 32);   // [2]
@@ -424,7 +426,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       set_error("split precision TSMM: real widths <= 64, or <= 128 out of place");
       return SKINNY_UNSUPPORTED;
     }
-    if (autoselect && (K < 8192 || !(cplx ? M * N >= 64 : (M >= 16 && N >= 16)))) {
+    if (autoselect && K < 8192) {
       set_error("split precision TSMM: not selected automatically for this shape");
       return SKINNY_UNSUPPORTED;
     }
@@ -438,10 +440,11 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       }
     return SKINNY_OK;
   }
-  // auto selection (measured on GB300, K with A of 1 GiB): FP64 split wins when both widths are
-  // >= 16 (1.07x at 16x16 .. 5x at 64x64); complex FP64 from M*N >= 64 (1.16x at 4x16, 5.2x at
-  // 32x32).  Below that the CUDA-core kernels are faster.  The autotuner can override.
-  const bool wins = cplx ? (M * N >= 64) : (Mr >= 16 && Nr >= 16);
+  // auto selection (measured on GB300, K with A of 1 GiB), on the real widths (complex doubled):
+  // split wins from Mr * Nr >= 256 with Nr >= 16 (real 8x32 1.48x, 16x16 1.75x, complex 4x16
+  // 1.47x, complex 8x8 1.77x, real 64x64 5x); narrower products stay on the CUDA-core kernels
+  // (real 8x8 0.86x, 16x4 0.70x, complex 16x4 0.97x).  The autotuner can override.
+  const bool wins = Mr * Nr >= 256 && Nr >= 16;
   if (autoselect && (K < 8192 || !wins)) {
     set_error("split precision TSMM: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
@@ -474,12 +477,17 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
     set_error("split precision TSMM: tiles do not fit in shared memory");
     return SKINNY_UNSUPPORTED;
   }
-  a.ntbuf = 2 * 8 * a.NM <= 512 ? 2 : 1;
-  a.tmem_cols = a.ntbuf * 8 * a.NM <= 256 ? 256 : 512;
+  // two CTAs per SM where a CTA fits half the TMEM and half the shared memory (contraction width
+  // 16: 128 registers); otherwise one CTA with two accumulator sets where they fit
+  const int smem_need = (int)(HDR + bdig + (int64_t)a.nabuf * a.abuf);
+  const bool two = MP <= 16 && 8 * a.NM <= 256 && 2 * smem_need <= h->dev.smem_optin;
+  a.ntbuf = two ? 256 / (8 * a.NM) : (2 * 8 * a.NM <= 512 ? 2 : 1);
+  a.tmem_cols = two ? 256 : (a.ntbuf * 8 * a.NM <= 256 ? 256 : 512);
   a.ntiles = (K + ROWS - 1) / ROWS;
   a.err = h->err;
   const int smem = (int)(HDR + bdig + (int64_t)a.nabuf * a.abuf);
-  int64_t grid = std::min<int64_t>(h->dev.sms, a.ntiles);
+  const int per_sm = two ? 2 : 1;
+  int64_t grid = std::min<int64_t>((int64_t)h->dev.sms * per_sm, a.ntiles);
   if (grid < 1) grid = 1;
   cudaError_t e;
   switch (MP) {
