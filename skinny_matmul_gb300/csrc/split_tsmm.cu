@@ -426,7 +426,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       set_error("split precision TSMM: real widths <= 64, or <= 128 out of place");
       return SKINNY_UNSUPPORTED;
     }
-    if (autoselect && K < 8192) {
+    if (autoselect && (K < 8192 || Nr < 16)) {
       set_error("split precision TSMM: not selected automatically for this shape");
       return SKINNY_UNSUPPORTED;
     }
