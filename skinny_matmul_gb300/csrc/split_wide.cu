@@ -410,9 +410,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       const int rs = ls % R, ds = ls % DSLOTS;
       const int64_t row0 = (s_begin + ls) * ROWS;
       const int rows = (int)min((int64_t)ROWS, p.K - row0);
-      wait_ab(&raw_full[rs], (uint32_t)((ls / R) & 1), abort_f, p.err);
-      // slot reuse: lane 0 waits for the MMAs that read the slot, then the warp writes it
-      if (ls >= DSLOTS && lane == 0) wait_ab(&dempty[ds], (uint32_t)(((ls / DSLOTS) - 1) & 1), abort_f, p.err);
+      // lane 0 waits for the FP64 stage (TMA) and for the MMAs that read the digit slot; the
+      // warp barrier then orders the other lanes' reads and writes after those waits
+      if (lane == 0) {
+        wait_ab(&raw_full[rs], (uint32_t)((ls / R) & 1), abort_f, p.err);
+        if (ls >= DSLOTS) wait_ab(&dempty[ds], (uint32_t)(((ls / DSLOTS) - 1) & 1), abort_f, p.err);
+      }
       __syncwarp();
       // load my unit and its column maximum
       const double* T = reinterpret_cast<const double*>(raw + (size_t)rs * p.raw_stage) + (isB ? ROWS * W : 0);
