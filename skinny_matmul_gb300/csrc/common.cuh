@@ -80,12 +80,15 @@ struct Ops<R, R> {  // float / double
   static __device__ __forceinline__ R mac(R acc, R a, R b) { return fma(a, b, acc); }
   static __device__ __forceinline__ R add(R x, R y) { return x + y; }
   static __device__ __forceinline__ bool is_zero(R v) { return v == R(0); }
-  // alpha == 1 skips the multiply (the same value: s * 1 == s); narrow TSMMs are bound by these
-  // epilogue operations on the FP64 pipe
   static __device__ __forceinline__ R finish(R s, R alpha, R beta, bool beta_zero, const R* c) {
-    const R as = alpha == R(1) ? s : s * alpha;
-    return beta_zero ? as : fma(*c, beta, as);
+    return beta_zero ? alpha * s : fma(*c, beta, s * alpha);
   }
+  // alpha == 1 (decided once per thread by the caller): the same value without the multiply;
+  // narrow TSMMs are bound by these epilogue operations on the FP64 pipe
+  static __device__ __forceinline__ R finish1(R s, R beta, bool beta_zero, const R* c) {
+    return beta_zero ? s : fma(*c, beta, s);
+  }
+  static __device__ __forceinline__ bool is_one(R a) { return a == R(1); }
   static __device__ __forceinline__ R shfl_xor(R v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 };
 
@@ -103,10 +106,14 @@ struct Ops<cplx<R>, cplx<R>> {
   static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
   static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
   static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
-    C r = (alpha.x == R(1) && alpha.y == R(0)) ? s : mul(alpha, s);
+    C r = mul(alpha, s);
     if (!beta_zero) r = add(mul(beta, *c), r);
     return r;
   }
+  static __device__ __forceinline__ C finish1(C s, C beta, bool beta_zero, const C* c) {
+    return beta_zero ? s : add(mul(beta, *c), s);
+  }
+  static __device__ __forceinline__ bool is_one(C a) { return a.x == R(1) && a.y == R(0); }
   static __device__ __forceinline__ C shfl_xor(C v, int o) {
     return {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
   }
@@ -126,10 +133,14 @@ struct Ops<cplxh<R>, cplxh<R>> {  // conj(a) * b per term (A^H B)
   static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
   static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
   static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
-    C r = (alpha.x == R(1) && alpha.y == R(0)) ? s : mul(alpha, s);
+    C r = mul(alpha, s);
     if (!beta_zero) r = add(mul(beta, *c), r);
     return r;
   }
+  static __device__ __forceinline__ C finish1(C s, C beta, bool beta_zero, const C* c) {
+    return beta_zero ? s : add(mul(beta, *c), s);
+  }
+  static __device__ __forceinline__ bool is_one(C a) { return a.x == R(1) && a.y == R(0); }
   static __device__ __forceinline__ C shfl_xor(C v, int o) {
     return {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
   }
@@ -149,6 +160,10 @@ struct Ops<double, dd> {  // double inputs, PseudoQuad accumulation
     }();
     return beta_zero ? v : __dadd_rn(__dmul_rn(beta, *c), v);
   }
+  static __device__ __forceinline__ double finish1(dd s, double beta, bool beta_zero, const double* c) {
+    return finish(s, 1.0, beta, beta_zero, c);
+  }
+  static __device__ __forceinline__ bool is_one(double) { return false; }
   static __device__ __forceinline__ dd shfl_xor(dd v, int o) {
     return {__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.t, o)};
   }

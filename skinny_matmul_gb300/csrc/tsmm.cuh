@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
   const int cell = threadIdx.x % gn, rs = threadIdx.x / gn;
   const int n0 = cell * TN;
   const int64_t step = (int64_t)gridDim.x * RS * U;
+  const bool alpha_one = O::is_one(p.alpha), bz = p.beta_zero != 0;  // decided once
   for (int64_t base = (int64_t)blockIdx.x * RS * U; base < p.K; base += step) {
     bool valid[U];
 #pragma unroll
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
     }
     __syncwarp();  // the whole rows have been read before any of them is overwritten (in place)
     T cv[U][TN];
-    if (!p.beta_zero) {  // C values of all U rows in flight together
+    if (!bz) {  // C values of all U rows in flight together
 #pragma unroll
       for (int j = 0; j < U; j++)
 #pragma unroll
@@ -93,7 +94,9 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
 #pragma unroll
       for (int u = 0; u < TN; u++) {
         const int n = n0 + u;
-        if (n < N) c_row[n] = O::finish(acc[j][u], p.alpha, p.beta, p.beta_zero != 0, &cv[j][u]);
+        if (n < N)
+          c_row[n] = alpha_one ? O::finish1(acc[j][u], p.beta, bz, &cv[j][u])
+                               : O::finish(acc[j][u], p.alpha, p.beta, bz, &cv[j][u]);
       }
     }
   }
