@@ -356,6 +356,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=2000, help="serve-c5: number of requests")
+    ap.add_argument("--store", default=None, help="append every measured shape to this JSONL results store")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload: skip the compact split-vs-FP64 and serving measurements")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve-c5: Poisson arrival rate per second")
@@ -469,6 +470,15 @@ def main():
             "served": srv, "one_launch_per_call": seq, "throughput_ratio": round(seq["wall_s"] / wall_srv, 3),
             "p99_ratio": round(srv["p99_ms"] / seq["p99_ms"], 3) if seq["p99_ms"] else None}
 
+    if rank == 0 and args.store:
+        from skinny_matmul_gb300 import results
+        device = torch.cuda.get_device_name(dev)
+        for it, r in zip(items, per):
+            results.record(args.store, {
+                "multype": it["op"].upper(), "device": device, "types": it["dt"], "M": it["M"], "N": it["N"],
+                "name": f"gb300-{args.method}", "inplace": int(it["inplace"]), "zerobeta": int(it["op"] == "tsmttsm"),
+                "K": it["K"], "time": r["us"] * 1e-6, "flops": r["TFLOP/s"] * 1e3, "bw": r["GB/s"],
+                "blockCount": 0})
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
