@@ -126,6 +126,13 @@ skinny_status skinny_svqb(skinny_handle handle, skinny_acc gram_acc, int64_t K, 
 skinny_status skinny_cholqr(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M, double* X, int64_t ldx,
                             int passes, double* orth_err_out, void* stream);
 
+/* SVQB of a complex FP64 block X (K x M, interleaved, M <= 64) in place: Hermitian Gram
+ * S = X^H X (skinny_tsmttsm_conj, method gram_acc), Hermitian Jacobi eigensolve on the device,
+ * X <- X (D^-1/2 U Lambda^-1/2) by the complex in-place TSMM.  No counterpart in the reference
+ * (its SVQB is real).  orth_err_out (nullable): ||Q^H Q - I||_F (synchronises the stream). */
+skinny_status skinny_svqb_z(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M, void* X, int64_t ldx,
+                            double* orth_err_out, void* stream);
+
 /* FP64 TSMTTSM that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: code that runs under an allocator owning the whole
  * device pool, or a latency-critical path where cudaMalloc's implicit device synchronisation is

@@ -61,3 +61,36 @@ def orth_error(Q: np.ndarray, K: int, M: int) -> float:
     """||Q^T Q - I||_F with the Gram formed exactly (svqb.cu:184-211 uses a double-double Gram)."""
     S = gram(Q, K, M, "exact")
     return float(np.linalg.norm(S - np.eye(M)))
+
+
+def make_x_complex(K: int, M: int, cond: float, seed: int = 0) -> np.ndarray:
+    """Complex X = G R: G complex Gaussian K x M, R upper triangular with singular values
+    log-spaced from 1 to 1/cond (as make_x, complex)."""
+    rng = np.random.default_rng(seed)
+    U, _ = np.linalg.qr(rng.standard_normal((M, M)) + 1j * rng.standard_normal((M, M)))
+    V, _ = np.linalg.qr(rng.standard_normal((M, M)) + 1j * rng.standard_normal((M, M)))
+    sig = np.logspace(0, -np.log10(cond), M)
+    _, R = np.linalg.qr(U @ np.diag(sig) @ V.conj().T)
+    G = rng.standard_normal((K, M)) + 1j * rng.standard_normal((K, M))
+    return np.ascontiguousarray(G @ R).ravel()
+
+
+def svqb_complex(X: np.ndarray, K: int, M: int) -> np.ndarray:
+    """Host SVQB of a complex block with the Hermitian Gram (test oracle of skinny_svqb_z):
+    S = X^H X, D^-1/2 scaling, eigendecomposition (LAPACK), eigenvalues ascending, each
+    eigenvector's largest-magnitude entry real positive, Q = X D U Lambda^-1/2."""
+    Xm = X.reshape(K, M)
+    S = Xm.conj().T @ Xm
+    sd = np.real(np.diag(S))
+    d = np.where(np.abs(sd) > 1e-15, 1.0 / np.sqrt(np.abs(sd)), 0.0)
+    w, U = np.linalg.eigh(S * d[:, None] * d[None, :])
+    for c in range(M):
+        k = int(np.argmax(np.abs(U[:, c])))
+        U[:, c] *= np.conj(U[k, c]) / abs(U[k, c])
+    T = (d[:, None] * U) / np.sqrt(np.maximum(1e-15, w))[None, :]
+    return (Xm @ T).ravel()
+
+
+def orth_error_complex(Q: np.ndarray, K: int, M: int) -> float:
+    Qm = Q.reshape(K, M)
+    return float(np.linalg.norm(Qm.conj().T @ Qm - np.eye(M)))

@@ -121,10 +121,12 @@ class Handle:
         return err.value if orth_err else None
 
     def svqb(self, K, M, X, ldx, gram_acc="split", orth_err=True, stream=None):
-        """In-place SVQB of X (K x M, FP64); returns ||Q^T Q - I||_F when orth_err."""
+        """In-place SVQB of X (K x M, FP64, or complex FP64 with the Hermitian Gram); returns
+        ||Q^H Q - I||_F when orth_err."""
         err = ctypes.c_double(-1.0)
-        L.check(self.lib.skinny_svqb(self.h, _ACC[gram_acc], K, M, _ptr(X), ldx,
-                                     ctypes.byref(err) if orth_err else None, _stream(stream)))
+        fn = self.lib.skinny_svqb_z if _dtype_code(X) == L.C64 else self.lib.skinny_svqb
+        L.check(fn(self.h, _ACC[gram_acc], K, M, _ptr(X), ldx, ctypes.byref(err) if orth_err else None,
+                   _stream(stream)))
         return err.value if orth_err else None
 
 

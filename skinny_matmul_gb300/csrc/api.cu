@@ -298,6 +298,25 @@ extern "C" skinny_status skinny_tsmm(skinny_handle h, skinny_dtype dt, skinny_ac
   return product(h, true, dt, acc, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, stream, nullptr);
 }
 
+namespace skinny {
+skinny_status dispatch_conj(skinny_handle h, skinny_dtype dt, skinny_acc acc, int64_t M, int64_t N, int64_t K,
+                            const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                            const void* beta, void* C, int64_t ldc, cudaStream_t st) {
+  LaunchOpts o{};
+  if (dt == SKINNY_C64 && (acc == SKINNY_ACC_SPLIT || acc == SKINNY_ACC_AUTO)) {
+    skinny_status s = split_complex_tsmttsm(h, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+                                            (double*)C, ldc, st, acc == SKINNY_ACC_AUTO, true);
+    if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
+  }
+  if (acc != SKINNY_ACC_NATIVE && acc != SKINNY_ACC_AUTO) {
+    set_error("method not provided for this dtype");
+    return SKINNY_UNSUPPORTED;
+  }
+  if (dt == SKINNY_C32) return run_t<c32h, c32h>(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+  return run_t<c64h, c64h>(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+}
+}  // namespace skinny
+
 // C = alpha A^H B + beta C (conjugate transpose; the reference has only the plain transpose,
 // tsmttsm/gen_cublas.cuh:29-39).  Real dtypes: the same as skinny_tsmttsm.
 extern "C" skinny_status skinny_tsmttsm_conj(skinny_handle h, skinny_dtype dt, skinny_acc acc, int64_t M,
@@ -315,20 +334,8 @@ extern "C" skinny_status skinny_tsmttsm_conj(skinny_handle h, skinny_dtype dt, s
   if (s != SKINNY_OK) return s;
   if (M == 0 || N == 0) return SKINNY_OK;
   DevGuard g(h->dev.id);
-  cudaStream_t st = (cudaStream_t)stream;
-  LaunchOpts o{};
   std::lock_guard<std::mutex> lk(h->mu);
-  if (dt == SKINNY_C64 && (acc == SKINNY_ACC_SPLIT || acc == SKINNY_ACC_AUTO)) {
-    s = split_complex_tsmttsm(h, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta, (double*)C, ldc,
-                              st, acc == SKINNY_ACC_AUTO, true);
-    if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
-  }
-  if (acc != SKINNY_ACC_NATIVE && acc != SKINNY_ACC_AUTO) {
-    set_error("method not provided for this dtype");
-    return SKINNY_UNSUPPORTED;
-  }
-  if (dt == SKINNY_C32) return run_t<c32h, c32h>(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
-  return run_t<c64h, c64h>(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+  return dispatch_conj(h, dt, acc, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, (cudaStream_t)stream);
 }
 
 // ----------------------------------------------------------------- reference-shaped wrappers

@@ -21,6 +21,7 @@ struct skinny_handle_st {
   std::map<cudaStream_t, void*> split_ws;                // split-precision scratch per stream
   std::map<cudaStream_t, size_t> split_ws_bytes;
   std::map<cudaStream_t, void*> svqb_ws;                 // SVQB scratch per stream
+  std::map<cudaStream_t, void*> svqbz_ws;                // complex SVQB scratch per stream
   int* err = nullptr;                                    // device error word (bounded waits)
 
   // launch options recorded by the autotuner for (op, dtype, acc, M, N); defaults otherwise
@@ -58,6 +59,11 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
                                int64_t M, int64_t N, int64_t K, const void* A, int64_t lda,
                                const void* alpha, const void* B, int64_t ldb, const void* beta,
                                void* C, int64_t ldc, cudaStream_t st, const LaunchOpts& o);
+
+// C = alpha A^H B + beta C for complex dtypes without checks or locking (caller holds h->mu).
+skinny_status dispatch_conj(skinny_handle h, skinny_dtype dt, skinny_acc acc, int64_t M, int64_t N, int64_t K,
+                            const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                            const void* beta, void* C, int64_t ldc, cudaStream_t st);
 
 // FP64 split-precision (tensor-core) products; SKINNY_UNSUPPORTED when the shape is not covered
 // (for auto == true the caller then falls back to the CUDA-core FP64 kernels).

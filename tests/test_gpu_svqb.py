@@ -64,3 +64,22 @@ def test_svqb_bad_arguments(handle):
         handle.svqb(10, 8, X, 4)
     with pytest.raises(SkinnyError, match="UNSUPPORTED"):
         handle.svqb(1, 65, dev(np.zeros(65)), 65)
+
+
+@pytest.mark.parametrize("M", [1, 5, 16, 40, 64])
+@pytest.mark.parametrize("gram", ["native", "split"])
+def test_complex_svqb_matches_oracle(handle, M, gram):
+    """Complex SVQB (Hermitian Gram, Hermitian Jacobi on the device) against the host oracle
+    (LAPACK eigensolver, the same phase convention)."""
+    K = 20000
+    X = OS.make_x_complex(K, M, 1e3, seed=M)
+    Xd = dev(X)
+    err = handle.svqb(K, M, Xd, M, gram_acc=gram)
+    torch.cuda.synchronize()
+    Q = Xd.cpu().numpy()
+    Qr = OS.svqb_complex(X, K, M)
+    rel = np.linalg.norm(Q - Qr) / np.linalg.norm(Qr)
+    assert rel <= 1e-9, rel
+    ref_err = OS.orth_error_complex(Q, K, M)
+    assert abs(err - ref_err) <= 1e-12 + 1e-6 * ref_err, (err, ref_err)
+    assert err <= 1e-10
