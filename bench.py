@@ -192,6 +192,8 @@ WORKLOADS = {
                    "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
     "tsmttsm-c1": (c1_items, "TSMTTSM FP64 C(8x8) = A^T B, K = 2^20, alpha 1, beta 0, "
                    "16 rotating input copies (2 GiB > L2)"),
+    "group-small": (c5_items, "the serving mix's small requests (TSMTTSM / TSMM of cost <= 32 MiB, FP64 / complex "
+                    "FP64 / FP32, operands in HBM): grouped launches vs one launch per request"),
     "serve-c5": (c5_items, "Poisson stream of TSMTTSM 50% / TSMM 35% / SVQB 15% requests, K log-uniform "
                  "[2^14, 2^24], M, N in {1..64}, FP64 60% / complex FP64 25% / FP32 15%, operands resident in "
                  "HBM; request loop vs one launch per call"),
@@ -362,6 +364,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve-c5: Poisson arrival rate per second")
     ap.add_argument("--streams", type=int, default=8, help="serve-c5: request-loop streams")
     ap.add_argument("--inflight", type=int, default=16, help="serve-c5: requests in flight at most")
+    ap.add_argument("--group-bytes", type=int, default=32 << 20,
+                    help="serve-c5: requests up to this many bytes run in grouped launches (0: off)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -371,6 +375,8 @@ def main():
         return run_svqb(args)
     if args.workload == "serve-c5":
         return run_serve(args)
+    if args.workload == "group-small":
+        return run_group(args)
 
     import torch
     from skinny_matmul_gb300 import Handle, build, lib
@@ -587,7 +593,7 @@ def c5_call(h, r, ops, stream=None):
         h.tsmm(r["M"], r["N"], r["K"], A, r["M"], 1.0, B, r["M"], 0.0, C, r["N"], acc=acc, stream=stream, dtype=dt)
 
 
-def serve_measure(h, dev, n, rate, rank, streams=8, inflight=16):
+def serve_measure(h, dev, n, rate, rank, streams=8, inflight=16, group_bytes=32 << 20):
     """Run the C5 stream both ways; returns (one-per-call stats, served stats, bytes, served wall)."""
     import numpy as np
     import torch
@@ -621,7 +627,7 @@ def serve_measure(h, dev, n, rate, rank, streams=8, inflight=16):
         return time.perf_counter() - t0, lat
 
     def served():
-        srv = Server(h, 120 * (1 << 30), num_streams=streams, max_inflight=inflight)
+        srv = Server(h, 120 * (1 << 30), num_streams=streams, max_inflight=inflight, group_bytes=group_bytes)
         tickets = []
         t0 = time.perf_counter()
         for i, (r, o) in enumerate(zip(reqs, ops)):
@@ -658,7 +664,8 @@ def serve_measure(h, dev, n, rate, rank, streams=8, inflight=16):
     srv = {"GB/s": round(total_bytes / wall_srv / 1e9, 1), "requests_per_s": round(n / wall_srv, 1),
            "p50_ms": round(st_srv["p50_latency_us"] / 1e3, 3), "p99_ms": round(st_srv["p99_latency_us"] / 1e3, 3),
            "wall_s": round(wall_srv, 3), "completed": int(st_srv["completed"]), "failed": int(st_srv["failed"]),
-           "max_inflight_seen": int(st_srv["max_inflight_seen"]),
+           "max_inflight_seen": int(st_srv["max_inflight_seen"]), "grouped": int(st_srv["grouped"]),
+           "group_launches": int(st_srv["group_launches"]), "group_bytes": int(group_bytes),
            "peak_bytes_in_use": int(st_srv["peak_bytes_in_use"])}
     del pools, ops
     torch.cuda.empty_cache()
@@ -682,7 +689,8 @@ def run_serve(args):
     n = args.requests
     n0 = L.skinny_kernel_launches()
     with ClockSampler(local) as clk:
-        seq, srv, total_bytes, wall_srv = serve_measure(h, dev, n, args.rate, rank, args.streams, args.inflight)
+        seq, srv, total_bytes, wall_srv = serve_measure(h, dev, n, args.rate, rank, args.streams, args.inflight,
+                                                        args.group_bytes)
     launches = L.skinny_kernel_launches() - n0
     h.check_device()
     value = sum_over_ranks(total_bytes / wall_srv / 1e9, world)
@@ -780,6 +788,103 @@ def run_svqb(args):
                 "svqb": rows, "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": None,
                 "e2e": None}
         print(json.dumps(line), flush=True)
+    h.close()
+
+
+# ------------------------------------------------------------------------------ grouped launches
+def c5_cost(r):
+    """A request's cost in bytes-equivalent as the request loop prices it for grouping: the larger
+    of its bytes and its FMAs at ~11.3 bytes per FP64 FMA (0.18 per FP32 FMA)."""
+    w = 4 if r["dt"] == "c64" else 1
+    fma = r["M"] * r["N"] * w * r["K"] + (r["N"] * w * r["K"] if r["op"] == "tsmm" else 0)
+    return max(r["bytes"], fma * (0.18 if r["dt"] == "f32" else 11.3))
+
+
+def run_group(args):
+    """The small requests of the serving mix (TSMTTSM / TSMM whose cost -- bytes, or FMAs priced at
+    the HBM-to-FMA rate ratio -- is at most 32 MiB; operands resident in HBM) run three ways: grouped launches (skinny_group, one per dtype
+    present), one launch per request back to back on one stream, and one launch per request with
+    a synchronisation after each (as a caller of the reference's launchers would).  Reports
+    algorithmic GB/s and microseconds per request of each."""
+    import numpy as np
+    import torch
+    from skinny_matmul_gb300 import Handle, build, lib
+    rank, world, local = dist_setup(args.gpus)
+    build.build()
+    h = Handle(torch.cuda.current_device())
+    L = lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = min(args.requests, 4096)
+    reqs = [r for r in c5_requests(40 * n, 4242 + rank) if r["op"] != "svqb" and c5_cost(r) <= (32 << 20)][:n]
+    pools = C5Pools(dev, 17 + rank)
+    ops = [pools.operands(r) for r in reqs]
+    by_dt = {}
+    for r, (A, B, C) in zip(reqs, ops):
+        lda = r["M"]
+        it = dict(op=r["op"], M=r["M"], N=r["N"], K=r["K"], A=A, lda=lda, B=B, ldb=r["N"] if r["op"] == "tsmttsm"
+                  else r["M"], C=C, ldc=r["M"] if r["op"] == "tsmttsm" else r["N"], alpha=1.0, beta=0.0)
+        by_dt.setdefault({"f64": "float64", "c64": "complex128", "f32": "float32"}[r["dt"]], []).append(it)
+    total_bytes = float(sum(r["bytes"] for r in reqs))
+
+    def grouped():
+        for dt, items in by_dt.items():
+            h.group(items, dtype=dt)
+
+    def one_stream():
+        for r, o in zip(reqs, ops):
+            c5_call(h, r, o)
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return sorted(ts)[len(ts) // 2]
+
+    n0 = L.skinny_kernel_launches()
+    with ClockSampler(local) as clk:
+        for _ in range(max(3, args.warmup)):
+            grouped()
+            one_stream()
+        torch.cuda.synchronize()
+        l0 = L.skinny_kernel_launches()
+        ms_g = timed(grouped, max(1, args.steps))
+        launches_g = (L.skinny_kernel_launches() - l0) // max(1, args.steps)
+        ms_s = timed(one_stream, max(1, args.steps))
+        t0 = time.perf_counter()
+        for r, o in zip(reqs, ops):
+            c5_call(h, r, o)
+            torch.cuda.synchronize()
+        ms_c = (time.perf_counter() - t0) * 1e3
+    launches = L.skinny_kernel_launches() - n0
+    h.check_device()
+    if rank == 0:
+        hbm, _ = peaks()
+        gbs = lambda ms: round(total_bytes / (ms * 1e-3) / 1e9, 1)
+        value = total_bytes / (ms_g * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms_g, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "mixed (f64, c64, f32)",
+                "data": "synthetic U[-1,1) operands resident in HBM, seeded",
+                "config": {"workload": "group-small", "description": WORKLOADS["group-small"][1], "requests": len(reqs),
+                           "bytes": total_bytes, "l2": "operands mostly L2-resident between steps (small requests)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "hbm", "achieved": round(value, 1), "peak": hbm, "unit": "GB/s",
+                             "frac": round(value / hbm, 4), "traffic": None, "kernel": "group_kernel"},
+                "group": {"grouped": {"ms": round(ms_g, 3), "GB/s": gbs(ms_g), "launches": int(launches_g),
+                                      "us_per_request": round(ms_g * 1e3 / len(reqs), 2)},
+                          "one_launch_per_request_one_stream": {"ms": round(ms_s, 3), "GB/s": gbs(ms_s),
+                                                                "us_per_request": round(ms_s * 1e3 / len(reqs), 2)},
+                          "one_launch_per_call_synchronised": {"ms": round(ms_c, 3), "GB/s": gbs(ms_c),
+                                                               "us_per_request": round(ms_c * 1e3 / len(reqs), 2)}},
+                "gpu_launches": int(launches), "clocks": clk.summary(), "cpu_baseline": None, "e2e": None}
+        print(json.dumps(line), flush=True)
+    del pools, ops
     h.close()
 
 

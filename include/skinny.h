@@ -199,6 +199,8 @@ typedef struct {
   double busy_seconds; /* wall time from the first admission to the last completion */
   uint64_t peak_bytes_in_use;
   uint64_t max_inflight_seen;
+  uint64_t grouped;        /* requests that ran in grouped launches */
+  uint64_t group_launches; /* grouped launches (graph replays) */
 } skinny_server_stats;
 
 typedef struct skinny_server_st* skinny_server;
@@ -215,6 +217,41 @@ skinny_status skinny_server_wait(skinny_server server, uint64_t ticket, skinny_s
 skinny_status skinny_server_drain(skinny_server server, double timeout_s);
 skinny_status skinny_server_stats_get(skinny_server server, skinny_server_stats* stats);
 skinny_status skinny_server_destroy(skinny_server server); /* drains first */
+/* Small requests -- TSMTTSM / TSMM with the native or auto method, M, N <= 64 and a cost of at
+ * most max_request_bytes, the cost being the larger of the request's algorithmic bytes and its
+ * FMAs priced at the dtype's HBM-to-FMA rate ratio (about 11 bytes per FP64 FMA on GB300) --
+ * do not take an in-flight slot: as they are admitted they
+ * are packed into grouped launches (skinny_group) of up to max_group requests, one launch per
+ * dtype present, replayed from instantiated CUDA graphs on a high-priority stream (the graph's
+ * descriptor copy and kernel nodes are updated and switched on or off per batch; two graphs
+ * alternate so that a batch is prepared while the previous one runs).  Small requests may pass a
+ * large one that waits for a slot, never one that waits for memory.  Default 32 MiB and 512;
+ * max_request_bytes = 0 turns grouping off (every request then runs as its own launch). */
+skinny_status skinny_server_set_grouping(skinny_server server, uint64_t max_request_bytes, int32_t max_group);
+
+/* ---- Grouped launches.  No counterpart in the reference.
+ * One persistent launch runs `count` small products of one dtype.  Each item is a TSMTTSM or a
+ * TSMM with the layouts and argument meaning of skinny_tsmttsm / skinny_tsmm (device pointers,
+ * in-place TSMM and Gram TSMTTSM included), M, N <= 64, any K; alpha and beta are (re, im)
+ * doubles, rounded to float for the FP32 dtypes.  Items' rows are cut into units spread over the
+ * grid; a TSMTTSM sums its units' partials in unit order inside the launch, so every result is
+ * deterministic and does not depend on the other items.  CUDA-core arithmetic in the working
+ * precision (the native method); a TSMM item gives the same bits as skinny_tsmm with the native
+ * method.  Items must not write memory that another item of the batch reads. */
+typedef struct {
+  skinny_op op; /* SKINNY_OP_TSMTTSM or SKINNY_OP_TSMM */
+  int64_t M, N, K;
+  const void* A;
+  int64_t lda;
+  const void* B;
+  int64_t ldb;
+  void* C;
+  int64_t ldc;
+  double alpha[2], beta[2];
+} skinny_group_item;
+
+skinny_status skinny_group(skinny_handle handle, skinny_dtype dtype, const skinny_group_item* items, int32_t count,
+                           void* stream);
 
 /* ---- Reference-shaped entry points ---------------------------------------------------------
  * Exactly MatmulFunctionType (versions.hpp:43-45).  They run on the legacy default stream with a

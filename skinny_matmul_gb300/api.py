@@ -120,6 +120,25 @@ class Handle:
                                        ctypes.byref(err) if orth_err else None, _stream(stream)))
         return err.value if orth_err else None
 
+    def group(self, items, dtype=None, stream=None):
+        """One grouped launch (skinny_group) of small products of one dtype.  `items` are dicts
+        with op ('tsmttsm' | 'tsmm'), M, N, K, A, lda, B, ldb, C, ldc and optional alpha (1),
+        beta (0); A, B, C device tensors or addresses.  dtype: 'float32' | 'float64' |
+        'complex64' | 'complex128' (default: from the first item's A)."""
+        if not items:
+            return L.OK
+        code = _DT[dtype] if dtype is not None else _dtype_code(items[0]["A"])
+        arr = (L.GroupItem * len(items))()
+        for g, it in zip(arr, items):
+            g.op = _OPS[it["op"]]
+            g.M, g.N, g.K = it["M"], it["N"], it["K"]
+            g.A, g.lda = _ptr(it["A"]), it["lda"]
+            g.B, g.ldb = _ptr(it["B"]), it["ldb"]
+            g.C, g.ldc = _ptr(it["C"]), it["ldc"]
+            a, b = complex(it.get("alpha", 1.0)), complex(it.get("beta", 0.0))
+            g.alpha[0], g.alpha[1], g.beta[0], g.beta[1] = a.real, a.imag, b.real, b.imag
+        return L.check(self.lib.skinny_group(self.h, code, arr, len(items), _stream(stream)))
+
     def svqb(self, K, M, X, ldx, gram_acc="split", orth_err=True, stream=None):
         """In-place SVQB of X (K x M, FP64, or complex FP64 with the Hermitian Gram); returns
         ||Q^H Q - I||_F when orth_err."""
@@ -189,13 +208,20 @@ class Server:
     the scheduler in dry mode (no device work)."""
 
     def __init__(self, handle: Handle | None, mem_budget_bytes: int, num_streams: int = 4,
-                 max_inflight: int = 16):
+                 max_inflight: int = 16, group_bytes: int | None = None, group_max: int = 512):
         self.lib = L.load()
         s = ctypes.c_void_p()
         L.check(self.lib.skinny_server_create(ctypes.byref(s), handle.h if handle else None,
                                               int(mem_budget_bytes), num_streams, max_inflight))
         self.s = s
         self._keep = {}
+        if group_bytes is not None:
+            self.set_grouping(group_bytes, group_max)
+
+    def set_grouping(self, max_request_bytes: int, max_group: int = 512):
+        """Requests up to max_request_bytes (TSMTTSM / TSMM, native or auto, M, N <= 64) run in
+        grouped launches of up to max_group; 0 turns grouping off."""
+        return L.check(self.lib.skinny_server_set_grouping(self.s, int(max_request_bytes), int(max_group)))
 
     def submit(self, op, dtype, M, N, K, A, lda, B=None, ldb=0, C=None, ldc=0, alpha=1.0, beta=0.0,
                acc="native", device=False):

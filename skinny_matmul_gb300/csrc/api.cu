@@ -123,6 +123,7 @@ extern "C" skinny_status skinny_destroy(skinny_handle h) {
     }
     for (void* p : h->extra_allocs) cudaFree(p);
     if (h->err) cudaFree(h->err);
+    group_release(h);
   }
   delete h;
   return SKINNY_OK;

@@ -89,4 +89,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
                          int64_t lda, const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
                          int64_t ldc, cudaStream_t st, bool autoselect);
 
+// Frees the grouped-launch buffers owned by a handle (group.cu).
+void group_release(skinny_handle h);
+
 }  // namespace skinny

@@ -43,7 +43,16 @@ class ServerStats(ctypes.Structure):
                 ("rejected", ctypes.c_uint64), ("p50_latency_us", ctypes.c_double),
                 ("p99_latency_us", ctypes.c_double), ("mean_latency_us", ctypes.c_double),
                 ("bytes", ctypes.c_double), ("busy_seconds", ctypes.c_double),
-                ("peak_bytes_in_use", ctypes.c_uint64), ("max_inflight_seen", ctypes.c_uint64)]
+                ("peak_bytes_in_use", ctypes.c_uint64), ("max_inflight_seen", ctypes.c_uint64),
+                ("grouped", ctypes.c_uint64), ("group_launches", ctypes.c_uint64)]
+
+
+class GroupItem(ctypes.Structure):
+    """skinny_group_item (include/skinny.h)."""
+    _fields_ = [("op", ctypes.c_int), ("M", ctypes.c_int64), ("N", ctypes.c_int64), ("K", ctypes.c_int64),
+                ("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
+                ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64),
+                ("alpha", ctypes.c_double * 2), ("beta", ctypes.c_double * 2)]
 
 
 OP_TSMTTSM, OP_TSMM, OP_SVQB = 0, 1, 2
@@ -90,6 +99,8 @@ SIGNATURES = {
     "skinny_server_drain": (_i, [_vp, ctypes.c_double]),
     "skinny_server_stats_get": (_i, [_vp, ctypes.POINTER(ServerStats)]),
     "skinny_server_destroy": (_i, [_vp]),
+    "skinny_server_set_grouping": (_i, [_vp, ctypes.c_uint64, ctypes.c_int32]),
+    "skinny_group": (_i, [_vp, _i, ctypes.POINTER(GroupItem), ctypes.c_int32, _vp]),
     "skinny_tsmttsm_d_static": (_i, [_i64, _i64, _i64, _vp, _i64, ctypes.c_double, _vp, _i64,
                                      ctypes.c_double, _vp, _i64, _vp]),
     "skinny_tsmttsm_s": (_i, _ref_sig(ctypes.c_float, ctypes.c_float)),

@@ -1,7 +1,9 @@
 """GPU tests of the request loop: a mixed stream of TSMTTSM / TSMM / SVQB requests in FP64,
 complex FP64 and FP32 runs through the server with several requests in flight, and every result
 is bit-identical to the same request run alone (the kernels are deterministic), and within the
-working precision's bound of the oracle."""
+working precision's bound of the oracle.  With grouping on, small requests run in grouped
+launches replayed from CUDA graphs; each of their results is bit-identical to the same item in a
+grouped launch of its own."""
 import numpy as np
 import pytest
 
@@ -70,7 +72,7 @@ def run_alone(handle, r):
 def test_mixed_stream_identical_alone_and_in_the_mix(handle):
     reqs = make_requests(11, 60)
     expected = [run_alone(handle, r) for r in reqs]
-    srv = Server(handle, 2 << 30, num_streams=4, max_inflight=12)
+    srv = Server(handle, 2 << 30, num_streams=4, max_inflight=12, group_bytes=0)
     tickets = []
     for r in reqs:
         if r["op"] == "svqb":
@@ -98,7 +100,7 @@ def test_mixed_stream_identical_alone_and_in_the_mix(handle):
 
 def test_served_results_match_oracle(handle):
     reqs = [r for r in make_requests(5, 30) if r["op"] == "tsmttsm" and r["dtype"] == "float64"][:6]
-    srv = Server(handle, 1 << 30)
+    srv = Server(handle, 1 << 30)  # grouping on (default): these small requests run grouped
     outs = []
     for r in reqs:
         C = r["C"].copy()
@@ -120,7 +122,7 @@ def test_device_resident_requests_identical_to_alone(handle):
     in flight; every result equals the same request run alone."""
     reqs = make_requests(23, 40)
     expected = [run_alone(handle, r) for r in reqs]
-    srv = Server(handle, 8 << 30, num_streams=4, max_inflight=8)
+    srv = Server(handle, 8 << 30, num_streams=4, max_inflight=8, group_bytes=0)
     outs, tickets = [], []
     for r in reqs:
         A = torch.from_numpy(r["A"].copy()).cuda()
@@ -140,4 +142,60 @@ def test_device_resident_requests_identical_to_alone(handle):
     assert stats["completed"] == len(reqs) and stats["max_inflight_seen"] >= 2
     for (A, B, C), r, e in zip(outs, reqs, expected):
         assert np.array_equal(C.cpu().numpy(), e), (r["op"], r["dtype"], r["M"], r["N"], r["K"])
+    srv.close()
+
+
+def _group_alone(handle, r):
+    """The same request as the only item of a grouped launch (device buffers via torch)."""
+    A = torch.from_numpy(r["A"].copy()).cuda()
+    B = A if r["B"] is r["A"] else torch.from_numpy(r["B"].copy()).cuda()
+    C = A if r["C"] is r["A"] else torch.from_numpy(r["C"].copy()).cuda()
+    handle.group([dict(op=r["op"], M=r["M"], N=r["N"], K=r["K"], A=A, lda=r["lda"], B=B, ldb=r["ldb"], C=C,
+                       ldc=r["ldc"], alpha=r["alpha"], beta=r["beta"])], dtype=r["dtype"])
+    torch.cuda.synchronize()
+    return C.cpu().numpy()
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_grouped_requests_identical_to_their_own_group(handle, device):
+    """Small requests (host or device operands) packed into graph-replayed grouped launches give
+    the bits of the same item alone in a grouped launch; large and SVQB requests still run on
+    their own in the same stream."""
+    reqs = make_requests(31 + device, 80)
+    expected = []
+    for r in reqs:
+        if r["op"] == "svqb":
+            expected.append(run_alone(handle, r))
+        else:
+            expected.append(_group_alone(handle, r))
+    # a threshold above every request's cost: every TSMTTSM / TSMM request runs grouped
+    srv = Server(handle, 4 << 30, num_streams=4, max_inflight=8, group_bytes=1 << 40, group_max=64)
+    outs, tickets = [], []
+    for r in reqs:
+        if device:
+            A = torch.from_numpy(r["A"].copy()).cuda()
+            if r["op"] == "svqb":
+                B, C = None, A
+            else:
+                B = A if r["B"] is r["A"] else torch.from_numpy(r["B"].copy()).cuda()
+                C = A if r["C"] is r["A"] else torch.from_numpy(r["C"].copy()).cuda()
+        else:
+            A = r["A"].copy()
+            B = None if r["op"] == "svqb" else (A if r["B"] is r["A"] else r["B"].copy())
+            C = A if (r["op"] == "svqb" or r["C"] is r["A"]) else r["C"].copy()
+        outs.append((A, B, C))
+        st, t = srv.submit(r["op"], r["dtype"], r["M"], r["N"], r["K"], A, r["lda"], B, r["ldb"], C, r["ldc"],
+                           r["alpha"], r["beta"], r["acc"], device=device)
+        assert st == L.OK
+        tickets.append(t)
+    for t in tickets:
+        assert srv.wait(t, 120) == (L.OK, L.OK)
+    stats = srv.stats()
+    n_small = sum(r["op"] != "svqb" for r in reqs)
+    assert stats["completed"] == len(reqs)
+    assert stats["grouped"] == n_small
+    assert 1 <= stats["group_launches"] <= n_small
+    for (A, B, C), r, e in zip(outs, reqs, expected):
+        got = C.cpu().numpy() if device else C
+        assert np.array_equal(got, e), (r["op"], r["dtype"], r["M"], r["N"], r["K"])
     srv.close()
