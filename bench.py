@@ -163,6 +163,15 @@ def probe_tsmm_items():
     return [it]
 
 
+def probe_tsmm64_items():
+    M = N = 64
+    K = 1 << 20
+    it = dict(op="tsmm", dt="f64", M=M, N=N, K=K, inplace=False, s=8)
+    it["bytes"] = tsmm_bytes(M, N, K, 8, False)
+    it["flops"] = (M * N * K + N * K) * 2
+    return [it]
+
+
 def probe_tsmttsm_items():
     M = N = 8
     K = 1 << 22
@@ -182,6 +191,8 @@ def probe_split_wide_items():
 
 
 WORKLOADS = {
+    "probe-split-tsmm64": (probe_tsmm64_items, "TSMM FP64 64x64, K = 2^20 (512 MiB A), alpha 1, beta 0.5, run "
+                           "with --method split: small case for ncu"),
     "probe-split-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-split": (probe_split_items, "TSMTTSM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-split-wide": (probe_split_wide_items, "TSMTTSM FP64 64x64, K = 2^21 (2 x 1 GiB), run with --method "
@@ -542,15 +553,16 @@ class C5Pools:
     pool, an SVQB pool (updated in place), and output scratch.  A request reads a slice of a pool at
     a seeded offset; outputs (alpha = 1, beta = 0) go to scratch that no request reads."""
 
-    def __init__(self, dev, seed):
+    def __init__(self, dev, seed, elems=(1 << 24) * 64 * 2, elems32=(1 << 24) * 64):
+        """elems / elems32: the largest FP64 (complex: two doubles per element) and FP32 operand of
+        any request (defaults: K = 2^24, width 64)."""
         import torch
         g = torch.Generator(device=dev).manual_seed(seed)
-        self.kmax = 1 << 24
-        n64 = self.kmax * 64 * 2 + (1 << 20)
+        n64 = elems + (1 << 20)
         self.p64 = torch.rand(n64, dtype=torch.float64, device=dev, generator=g) * 2 - 1
-        self.p32 = torch.rand(self.kmax * 64 + (1 << 20), dtype=torch.float32, device=dev, generator=g) * 2 - 1
-        self.psv = torch.randn(self.kmax * 64 * 3, dtype=torch.float64, device=dev, generator=g)
-        self.out = torch.empty(self.kmax * 64 * 2, dtype=torch.float64, device=dev)
+        self.p32 = torch.rand(elems32 + (1 << 20), dtype=torch.float32, device=dev, generator=g) * 2 - 1
+        self.psv = torch.randn(elems * 3 // 2, dtype=torch.float64, device=dev, generator=g)
+        self.out = torch.empty(elems, dtype=torch.float64, device=dev)
         self.outs = torch.empty(1 << 16, dtype=torch.float64, device=dev)
 
     def slice(self, pool, count, u):
@@ -816,7 +828,10 @@ def run_group(args):
     dev = torch.device("cuda", torch.cuda.current_device())
     n = min(args.requests, 4096)
     reqs = [r for r in c5_requests(40 * n, 4242 + rank) if r["op"] != "svqb" and c5_cost(r) <= (32 << 20)][:n]
-    pools = C5Pools(dev, 17 + rank)
+    w = lambda r: 2 if r["dt"] == "c64" else 1
+    need = [r["K"] * max(r["M"], r["N"]) * w(r) for r in reqs]
+    pools = C5Pools(dev, 17 + rank, elems=max(need),
+                    elems32=max([n for n, r in zip(need, reqs) if r["dt"] == "f32"] or [1]))
     ops = [pools.operands(r) for r in reqs]
     by_dt = {}
     for r, (A, B, C) in zip(reqs, ops):

@@ -15,13 +15,19 @@
 //     product of the last (L-1) planes of A' with the first (L-1) planes of B' pairs exactly the
 //     digits with i + j = L, so one MMA chain per level gives D_L(r, n) = sum_{i+j=L} sum_m a_i b_j.
 //   * |D_L| <= 8 * MP * 2^14 <= 2^23: exact in the FP32 TMEM accumulator.
-//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers, its top 61+ bits (from its
-//     own leading bit; the rest lies below 2^-61 of |V|) are rounded to a double with integer
-//     instructions and scaled by 2^(e_r + f_n - 2112) in the exponent field; beta*C is one FMA.
+//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers (level pairs in 32 bits),
+//     its top 61+ bits (from its own leading bit; the rest lies below 2^-61 of |V|) are rounded to
+//     a double with integer instructions and scaled by 2^(e_r + f_n - 2112) in the exponent field;
+//     beta*C is one FMA (the only FP64-pipe operation per output).
 //     Levels >= 10 are dropped (weight below 2^-56 of the leading level).
-//   * Tiles of 128 rows: two threads per row read the row's FP64 values straight from global
-//     memory into registers (the next tile is prefetched while the current one is sliced); the
+//   * Tiles of 128 rows: two threads per row (contraction width 16; four above, with 16 warps per
+//     CTA) read the row's FP64 values straight from global memory into registers; the next
+//     tile's values are loaded right after the current one is sliced, behind the epilogue; the
 //     MMAs of tile t overlap the epilogue of tile t-1 where two TMEM accumulators fit (N <= 32).
+//     Four threads issue the level chains (levels 2+w and 9-w from warp w: 9*MP/16 MMAs each), so
+//     no single warp serialises the whole tile's MMAs.  The epilogue reads the old C values of a
+//     chunk before the TMEM loads of the chunk before it (16-byte pieces where rows are aligned),
+//     so that global and TMEM latencies overlap.
 //   * |D_L| <= 2^22 for contraction widths <= 32 (converted with a float add), <= 2^23 for 64
 //     (converted with cvt.rni); both exact.
 // Complex FP64 (interleaved) runs as the real product of doubled width: A (K x 2M), B' (2M x 2N)
@@ -37,9 +43,12 @@ namespace skinny {
 namespace stsmm {
 
 constexpr int ROWS = 128;
-constexpr int THREADS = 256;
+// threads: 256 when two CTAs share an SM (contraction width 16, accumulators of <= 256 columns),
+// otherwise 512 (one CTA of 16 warps per SM); 128 registers either way.  Rows are sliced by up to
+// four threads each (8 columns at least per thread); the epilogue splits the columns over NT/128
+// warp groups -- enough warps to cover its TMEM and global latencies.
 constexpr int DIGITS = 8;
-constexpr int HDR = 4096;      // barriers, TMEM slot, row/column exponents
+constexpr int HDR = 8192;      // barriers, TMEM slot, row/column exponents
 
 struct Args {
   const double* A;
@@ -51,6 +60,7 @@ struct Args {
   int cplx;                  // B is complex (alpha, beta complex)
   double alpha[2], beta[2];
   int beta_zero, inplace, vec;  // vec: rows of A may be read as 16-byte pairs
+  int vecc;                     // rows of C may be read and written as 16-byte pairs
   int64_t ntiles;
   uint32_t abuf;  // bytes of one A' buffer
   int nabuf;      // A' buffers (1 or 2)
@@ -166,14 +176,16 @@ __device__ __forceinline__ double i64_to_double(long long x, int E) {
 
 // contraction width 16 (TMEM <= 256 columns, shared memory < 114 KB): two CTAs per SM, so that one
 // CTA's barriers overlap the other's work
-template <int MP>
-__global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(const Args p) {
-  constexpr int HALF = MP / 2;  // columns sliced per thread (two threads per row)
+template <int MP, int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const Args p) {
+  constexpr int TPR = NT / ROWS;                         // column parts of the epilogue
+  constexpr int TPS = MP / 8 < TPR ? MP / 8 : TPR;       // threads slicing a row
+  constexpr int PART = MP / TPS;                         // columns sliced per thread
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bar_mma = reinterpret_cast<uint64_t*>(smem + 32);   // [2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
-  int* erow = reinterpret_cast<int*>(smem + 128);               // [2 parity][2 halves][ROWS]
-  int* fcol = reinterpret_cast<int*>(smem + 128 + 4 * ROWS * 4);  // [64]
+  int* erow = reinterpret_cast<int*>(smem + 128);               // [2 parity][TPR parts][ROWS]
+  int* fcol = reinterpret_cast<int*>(smem + 128 + 2 * TPR * ROWS * 4);  // [64]
   const int M = p.M, N = p.N, NM = p.NM;
   const uint32_t lbo_a = ROWS * 16, lbo_b = (uint32_t)NM * 16;
   unsigned char* bdig = smem + HDR;                               // B' (NM x 8*MP), 1024-aligned
@@ -190,9 +202,9 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
                  "r"(p.tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) {
-    mbar_init(&bar_mma[0], 1);
-    mbar_init(&bar_mma[1], 1);
+  if (tid == 0) {  // four issuing threads commit to each tile's barrier
+    mbar_init(&bar_mma[0], 4);
+    mbar_init(&bar_mma[1], 4);
     fence_mbar_init();
   }
   // ---- B' = digits of alpha * B: column exponents, then (n, m-octet) units -------------------
@@ -202,7 +214,7 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
     fcol[tid] = (int)f;
   }
   __syncthreads();
-  for (int u = tid; u < NM * (MP / 8); u += THREADS) {
+  for (int u = tid; u < NM * (MP / 8); u += NT) {
     const int n = u % NM, mo = u / NM;
     float d[8][DIGITS];
     bool ng[8];
@@ -221,8 +233,9 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
   const uint32_t tmem = *tslot;
 
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NM >> 3) << 17) | ((128u >> 4) << 24);
-  const int row = tid & (ROWS - 1), half = tid >> 7;
-  const int m0 = half * HALF;
+  const int row = tid & (ROWS - 1), part = tid >> 7;
+  const bool slicer = part < TPS;
+  const int m0 = (slicer ? part : 0) * PART;
   int uses[2] = {0, 0};
   bool bail = false;
 
@@ -232,25 +245,50 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
     const int rows = (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS);
     const int q = warp & 3;
     const int r = 32 * q + lane;
-    const int* er = erow + ((it & 1) * 2) * ROWS;
+    const int* er = erow + ((it & 1) * TPR) * ROWS;
     const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((it % p.ntbuf) * 8 * NM);
-    const int nh = min(N, (((N + 1) / 2) + 1) & ~1);  // even split keeps complex (re, im) pairs together
-    const int n0 = (warp < 4) ? 0 : nh, n1 = (warp < 4) ? nh : N;
-    for (int c0 = (n0 & ~7); c0 < n1; c0 += 8) {
-      uint32_t raw[8][8];
+    // TPR column parts of even width (complex (re, im) pairs stay together), one per warp group
+    const int pw = ((N + TPR - 1) / TPR + 1) & ~1;
+    const int n0 = min(N, (warp >> 2) * pw), n1 = min(N, n0 + pw);
+    const bool live = r < rows;
+    double* crow = p.C + (r0 + r) * p.ldc;
+    // a chunk of 8 columns inside [n0, n1) is moved as four 16-byte pieces when C's rows allow it
+    auto whole = [&](int c0) { return p.vecc && c0 >= n0 && c0 + 8 <= n1; };
+    // old C values of a chunk (in place: this row of A, not yet overwritten); issued before the
+    // TMEM loads of the chunk before it, so that the global and TMEM latencies overlap
+    auto load_c = [&](int c0, double (&cv)[8]) {
+      if (p.beta_zero || !live) {
 #pragma unroll
-      for (int L = 0; L < 8; L++) tmem_ld8(tbase + (uint32_t)(L * NM + c0), raw[L]);
-      tmem_wait();
-      if (r < rows) {
-        const int e = er[r];
-        double* crow = p.C + (r0 + r) * p.ldc;
-        // old C values of the chunk (in place: this row of A, not yet overwritten) before any write
-        double cold[8];
+        for (int x = 0; x < 8; x++) cv[x] = 0.0;
+      } else if (whole(c0)) {
+#pragma unroll
+        for (int x = 0; x < 8; x += 2) {
+          const double2 w = *reinterpret_cast<const double2*>(crow + c0 + x);
+          cv[x] = w.x;
+          cv[x + 1] = w.y;
+        }
+      } else {
 #pragma unroll
         for (int x = 0; x < 8; x++) {
           const int n = c0 + x;
-          cold[x] = (!p.beta_zero && n >= n0 && n < n1) ? crow[n] : 0.0;
+          cv[x] = (n >= n0 && n < n1) ? crow[n] : 0.0;
         }
+      }
+    };
+    // 128 registers: no room for a second chunk of C, so a chunk's own C loads go out just
+    // before its TMEM loads
+    constexpr bool AHEAD = false;
+    double cold[8], cnext[8];
+    if (AHEAD && n0 < n1) load_c(n0 & ~7, cold);
+    for (int c0 = (n0 & ~7); c0 < n1; c0 += 8) {
+      if (!AHEAD) load_c(c0, cold);
+      uint32_t raw[8][8];
+#pragma unroll
+      for (int L = 0; L < 8; L++) tmem_ld8(tbase + (uint32_t)(L * NM + c0), raw[L]);
+      if (AHEAD && c0 + 8 < n1) load_c(c0 + 8, cnext);
+      tmem_wait();
+      if (live) {
+        const int e = er[r];
         double out[8];
 #pragma unroll
         for (int x = 0; x < 8; x++) {
@@ -262,15 +300,21 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
 #pragma unroll
           for (int L = 0; L < 8; L++) {
             const float f = __uint_as_float(raw[L][x]);
-            dl[L] = MP <= 32 ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
+            // |D_L| <= (L-1) * MP * 2^14: up to 2^22 the magic add is exact (levels 2..5 at MP = 64)
+            dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
           }
+          // level pairs in 32 bits: |D_L| <= (L-1) * MP * 2^14, so |D_L * 256 + D_{L+1}| < 2^31 for
+          // every pair (the largest, D_8 * 256 + D_9 at MP = 64, is below 1.9e9)
+          const int P1 = dl[0] * 256 + dl[1], P2 = dl[2] * 256 + dl[3];
+          const int P3 = dl[4] * 256 + dl[5], P4 = dl[6] * 256 + dl[7];
           // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
-          const long long H = ((long long)dl[0] * 256 + dl[1]) * 65536 + ((long long)dl[2] * 256 + dl[3]);
-          const long long Lo = ((long long)dl[4] * 256 + dl[5]) * 65536 + ((long long)dl[6] * 256 + dl[7]);
+          const long long H = ((long long)P1 << 16) + P2;
+          const long long Lo = ((long long)P3 << 16) + P4;
           // the top bits of V from its own leading bit: shift H up by k = clz(|H|) - 2, so that
           // |H << k| < 2^62 and adding the |Lo| part (< 2^48) cannot pass 2^63 (k = 32: V fits in
           // 64 bits and is kept whole); at least 61 bits are kept, the bits of Lo dropped lie below
-          // 2^-61 of |V|
+          // 2^-61 of |V|.  They are rounded to a double with integer instructions (a conversion
+          // instruction from 64-bit integers runs on the FP64 pipe, the scarce unit here)
           const long long aH = H < 0 ? -H : H;
           const int k = aH ? min(32, __clzll(aH) - 2) : 32;
           const long long top = (H << k) + (Lo >> (32 - k));
@@ -285,11 +329,20 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
           }
           out[x] = v;
         }
+        if (whole(c0)) {
 #pragma unroll
-        for (int x = 0; x < 8; x++) {
-          const int n = c0 + x;
-          if (n >= n0 && n < n1) crow[n] = out[x];
+          for (int x = 0; x < 8; x += 2) *reinterpret_cast<double2*>(crow + c0 + x) = make_double2(out[x], out[x + 1]);
+        } else {
+#pragma unroll
+          for (int x = 0; x < 8; x++) {
+            const int n = c0 + x;
+            if (n >= n0 && n < n1) crow[n] = out[x];
+          }
         }
+      }
+      if (AHEAD) {
+#pragma unroll
+        for (int x = 0; x < 8; x++) cold[x] = cnext[x];
       }
     }
   };
@@ -298,26 +351,27 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
     return mbar_wait_bounded(&bar_mma[b], (uint32_t)((uses[b] - 1) & 1), p.err);
   };
 
-  double v[HALF], vn[HALF];
-  if (nt > 0) {
-    const int64_t r0 = t_begin * ROWS;
-    load_row<HALF>(p, r0, row, (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS), m0, v);
-  }
+  // A values of the tile being sliced; the next tile's are loaded into the same registers right
+  // after slicing (the old values are dead then), so their latency hides behind the epilogue
+  double v[PART];
+  auto load_tile = [&](int it) {
+    const int64_t r1 = (t_begin + it) * ROWS;
+    load_row<PART>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, v);
+  };
+  if (nt > 0 && slicer) load_tile(0);
   for (int it = 0; it < nt && !bail; it++) {
-    const int64_t t = t_begin + it;
-    const int64_t r0 = t * ROWS;
-    if (it + 1 < nt) {  // prefetch the next tile's values into registers
-      const int64_t r1 = r0 + ROWS;
-      load_row<HALF>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, vn);
-    }
-    // row exponents: each half of the columns, combined through shared memory
-    uint32_t emax = 0;
+    // row exponents: each part of the columns, combined through shared memory
+    int* er = erow + ((it & 1) * TPR) * ROWS;
+    if (slicer) {
+      uint32_t emax = 0;
 #pragma unroll
-    for (int j = 0; j < HALF; j++) emax = max(emax, exp_field(v[j]));
-    int* er = erow + ((it & 1) * 2) * ROWS;
-    er[half * ROWS + row] = (int)emax;
+      for (int j = 0; j < PART; j++) emax = max(emax, exp_field(v[j]));
+      er[part * ROWS + row] = (int)emax;
+    }
     __syncthreads();
-    const int e_row = max(er[row], er[ROWS + row]);
+    int e_row = er[row];
+#pragma unroll
+    for (int q2 = 1; q2 < TPS; q2++) e_row = max(e_row, er[q2 * ROWS + row]);
     // the A' buffer is free once the MMAs that read it completed
     if ((p.nabuf == 1 && it > 0) || (p.nabuf == 2 && it > 1)) {
       bool ok = wait_mma(it - p.nabuf);
@@ -328,7 +382,7 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
     }
     unsigned char* A_ = adig + (size_t)(it % p.nabuf) * p.abuf;
 #pragma unroll
-    for (int o = 0; o < HALF / 8; o++) {
+    for (int o = 0; o < (slicer ? PART / 8 : 0); o++) {
       const int mo = (m0 >> 3) + o;
       if (mo * 8 >= M) {  // zero padding columns: zero digits
 #pragma unroll
@@ -350,9 +404,16 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
     }
     if (tid < ROWS) er[tid] = e_row;  // the epilogue of this tile reads er[r]
     fence_proxy_async_smem();
-    tc_before();
-    __syncthreads();
-    if (p.ntbuf == 1 && it > 0) {  // one accumulator: drain tile it-1 before tile it's MMAs
+    // one accumulator: the epilogue of tile it-1 needs no barrier after this tile's slicing (it
+    // reads TMEM and C, not A'), so warps go from slicing straight into it; the barrier that
+    // ends the epilogue also completes A' for the MMAs
+    const bool drain_first = p.ntbuf == 1 && it > 0;
+    if (!drain_first) {
+      tc_before();
+      __syncthreads();
+    }
+    if (it + 1 < nt && slicer) load_tile(it + 1);  // in flight during the epilogue and the MMAs
+    if (drain_first) {  // one accumulator: drain tile it-1 before tile it's MMAs
       if (p.nabuf != 1) {
         bool ok = wait_mma(it - 1);
         if (__syncthreads_or(!ok)) {
@@ -365,18 +426,20 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
       tc_before();
       __syncthreads();
     }
-    if (tid == 0) {
+    if (lane == 0 && warp < 4) {  // warp w issues the chains of levels 2 + w and 9 - w (9 K-steps of MP/16)
       tc_after();
       const uint32_t a0 = smem_u32(A_), b0 = smem_u32(bdig);
       const uint32_t dcol = tmem + (uint32_t)((it % p.ntbuf) * 8 * NM);
-      for (int L = 2; L <= 9; L++) {
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        const int L = side ? 9 - warp : 2 + warp;
         const int kq = (L - 1) * MP / 16;  // K-steps of 16
         const int ka = (9 - L) * MP / 8;   // first k-octet of A' for this level
         for (int ks = 0; ks < kq; ks++)
           mma_bf16(dcol + (uint32_t)((L - 2) * NM), make_desc(a0 + (uint32_t)(ka + 2 * ks) * lbo_a, lbo_a),
                    make_desc(b0 + (uint32_t)(2 * ks) * lbo_b, lbo_b), idesc, ks > 0 ? 1u : 0u);
       }
-      mma_commit(&bar_mma[it & 1]);
+      mma_commit(&bar_mma[it & 1]);  // one of the four arrivals that complete the tile's phase
     }
     uses[it & 1]++;
     if (p.ntbuf == 2 && it > 0) {  // the previous tile's epilogue overlaps this tile's MMAs
@@ -390,8 +453,6 @@ __global__ void __launch_bounds__(THREADS, MP <= 16 ? 2 : 1) split_tsmm_kernel(c
       tc_before();
       __syncthreads();
     }
-#pragma unroll
-    for (int j = 0; j < HALF; j++) v[j] = vn[j];
   }
   if (!bail && nt > 0) {
     bool ok = wait_mma(nt - 1);
@@ -426,7 +487,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       set_error("split precision TSMM: real widths <= 64, or <= 128 out of place");
       return SKINNY_UNSUPPORTED;
     }
-    if (autoselect && (K < 8192 || Nr < 16)) {
+    if (autoselect && (K < 8192 || Nr < 16 || Mr < 8)) {
       set_error("split precision TSMM: not selected automatically for this shape");
       return SKINNY_UNSUPPORTED;
     }
@@ -440,11 +501,12 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       }
     return SKINNY_OK;
   }
-  // auto selection (measured on GB300, K with A of 1 GiB), on the real widths (complex doubled):
-  // split wins from Mr * Nr >= 256 with Nr >= 16 (real 8x32 1.48x, 16x16 1.75x, complex 4x16
-  // 1.47x, complex 8x8 1.77x, real 64x64 5x); narrower products stay on the CUDA-core kernels
-  // (real 8x8 0.86x, 16x4 0.70x, complex 16x4 0.97x).  The autotuner can override.
-  const bool wins = Mr * Nr >= 256 && Nr >= 16;
+  // auto selection (measured on GB300, K with A of 1 GiB, and over every C5 width pair with ~512
+  // MB operands), on the real widths (complex doubled): split wins from Mr * Nr >= 256 with
+  // Nr >= 16 and a contraction width Mr >= 8 (real 8x32 1.4x, 16x16 1.6x, complex 4x16 1.4x,
+  // complex 8x8 1.6x, real 64x64 6x); narrower products stay on the CUDA-core kernels (real 8x8
+  // 0.66x, real 4x64 0.67x, complex 1x64 0.35x, complex 2x32 0.64x).  The autotuner can override.
+  const bool wins = Mr * Nr >= 256 && Nr >= 16 && Mr >= 8;
   if (autoselect && (K < 8192 || !wins)) {
     set_error("split precision TSMM: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
@@ -469,6 +531,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   a.beta_zero = a.beta[0] == 0.0 && a.beta[1] == 0.0;
   a.inplace = (const void*)A == (const void*)C;
   a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
+  a.vecc = ((uintptr_t)C % 16 == 0) && (a.ldc % 2 == 0);
   a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x bf16
   const int64_t bdig = round_up((int64_t)8 * MP * a.NM * 2, 1024);
   const int64_t avail = h->dev.smem_optin - HDR - bdig;
@@ -491,22 +554,27 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   if (grid < 1) grid = 1;
   cudaError_t e;
   switch (MP) {
-    case 16: {
-      static std::atomic<int> attr{0};
-      ensure_smem_attr(split_tsmm_kernel<16>, smem, attr);
-      split_tsmm_kernel<16><<<(int)grid, THREADS, smem, st>>>(a);
+    case 16:
+      if (two) {
+        static std::atomic<int> attr{0};
+        ensure_smem_attr(split_tsmm_kernel<16, 256>, smem, attr);
+        split_tsmm_kernel<16, 256><<<(int)grid, 256, smem, st>>>(a);
+      } else {
+        static std::atomic<int> attr{0};
+        ensure_smem_attr(split_tsmm_kernel<16, 512>, smem, attr);
+        split_tsmm_kernel<16, 512><<<(int)grid, 512, smem, st>>>(a);
+      }
       break;
-    }
     case 32: {
       static std::atomic<int> attr{0};
-      ensure_smem_attr(split_tsmm_kernel<32>, smem, attr);
-      split_tsmm_kernel<32><<<(int)grid, THREADS, smem, st>>>(a);
+      ensure_smem_attr(split_tsmm_kernel<32, 512>, smem, attr);
+      split_tsmm_kernel<32, 512><<<(int)grid, 512, smem, st>>>(a);
       break;
     }
     default: {
       static std::atomic<int> attr{0};
-      ensure_smem_attr(split_tsmm_kernel<64>, smem, attr);
-      split_tsmm_kernel<64><<<(int)grid, THREADS, smem, st>>>(a);
+      ensure_smem_attr(split_tsmm_kernel<64, 512>, smem, attr);
+      split_tsmm_kernel<64, 512><<<(int)grid, 512, smem, st>>>(a);
       break;
     }
   }
