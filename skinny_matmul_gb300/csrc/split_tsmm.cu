@@ -159,19 +159,51 @@ __device__ __forceinline__ void load_row(const Args& p, int64_t r0, int row, int
   }
 }
 
-// x * 2^E for a signed 64-bit integer x, rounded to 53 bits (ties away from zero); |x| < 2^63.
+// x * 2^E for a signed 64-bit integer x, rounded to 53 bits (ties away from zero); |x| < 2^63,
+// 0 for x == 0.  Branch-free: for x == 0 the normalising shift is masked to 0 and the final select
+// returns 0.
 __device__ __forceinline__ double i64_to_double(long long x, int E) {
-  if (x == 0) return 0.0;
   const unsigned long long sgn = (unsigned long long)x & 0x8000000000000000ull;
   unsigned long long m = (unsigned long long)(x < 0 ? -x : x);
-  const int z = __clzll((long long)m);  // >= 1
-  m <<= z;                              // leading one at bit 63
+  const int z = __clzll((long long)m);  // >= 1 for x != 0
+  m <<= (z & 63);                       // leading one at bit 63
   unsigned long long mant = (m + 0x400ull) >> 11;  // round on bit 10; may carry to 2^53
   int ex = 63 - z + E;
   const unsigned long long carry = mant >> 53;
   mant >>= carry;
   ex += (int)carry;
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  const double r =
+      __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  return x ? r : 0.0;
+}
+
+// The double of column x of a chunk: V = sum_L D_L 2^(8(9-L)) from the eight FP32 level sums in
+// raw[L][x] (exact integers), times 2^E.
+template <int MP>
+__device__ __forceinline__ double level_value(const uint32_t (&raw)[8][8], int x, int E) {
+  int dl[8];
+#pragma unroll
+  for (int L = 0; L < 8; L++) {
+    const float f = __uint_as_float(raw[L][x]);
+    // |D_L| <= (L-1) * MP * 2^14: up to 2^22 the magic add is exact (levels 2..5 at MP = 64)
+    dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
+  }
+  // level pairs in 32 bits: |D_L * 256 + D_{L+1}| < 2^31 for every pair (the largest, D_8 * 256 +
+  // D_9 at MP = 64, is below 1.9e9)
+  const int P1 = dl[0] * 256 + dl[1], P2 = dl[2] * 256 + dl[3];
+  const int P3 = dl[4] * 256 + dl[5], P4 = dl[6] * 256 + dl[7];
+  // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
+  const long long H = ((long long)P1 << 16) + P2;
+  const long long Lo = ((long long)P3 << 16) + P4;
+  // the top bits of V from its own leading bit: shift H up by k = clz(|H|) - 2, so that
+  // |H << k| < 2^62 and adding the |Lo| part (< 2^48) cannot pass 2^63 (k = 32, also for H = 0:
+  // V fits in 64 bits and is kept whole); at least 61 bits are kept, the bits of Lo dropped lie
+  // below 2^-61 of |V|.  They are rounded to a double with integer instructions (a conversion
+  // instruction from 64-bit integers runs on the FP64 pipe, the scarce unit here)
+  const long long aH = H < 0 ? -H : H;
+  const int k = min(32, __clzll(aH) - 2);
+  const long long top = (H << k) + (Lo >> (32 - k));
+  return i64_to_double(top, E - k);
 }
 
 // contraction width 16 (TMEM <= 256 columns, shared memory < 114 KB): two CTAs per SM, so that one
@@ -288,46 +320,24 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const
       if (AHEAD && c0 + 8 < n1) load_c(c0 + 8, cnext);
       tmem_wait();
       if (live) {
-        const int e = er[r];
+        // all eight columns are formed (columns beyond N hold zero digits and exponent 0) and
+        // masked only at the store; beta * C with the dtype test outside the column loop
+        const int e = er[r] - 2112 + 32;
         double out[8];
 #pragma unroll
-        for (int x = 0; x < 8; x++) {
-          const int n = c0 + x;
-          out[x] = 0.0;
-          if (n < n0 || n >= n1) continue;
-          // level sums as integers (float-to-int by a magic add where |D_L| <= 2^22)
-          int dl[8];
+        for (int x = 0; x < 8; x++) out[x] = level_value<MP>(raw, x, e + fcol[c0 + x]);
+        if (!p.beta_zero) {
+          if (!p.cplx) {
 #pragma unroll
-          for (int L = 0; L < 8; L++) {
-            const float f = __uint_as_float(raw[L][x]);
-            // |D_L| <= (L-1) * MP * 2^14: up to 2^22 the magic add is exact (levels 2..5 at MP = 64)
-            dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
-          }
-          // level pairs in 32 bits: |D_L| <= (L-1) * MP * 2^14, so |D_L * 256 + D_{L+1}| < 2^31 for
-          // every pair (the largest, D_8 * 256 + D_9 at MP = 64, is below 1.9e9)
-          const int P1 = dl[0] * 256 + dl[1], P2 = dl[2] * 256 + dl[3];
-          const int P3 = dl[4] * 256 + dl[5], P4 = dl[6] * 256 + dl[7];
-          // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
-          const long long H = ((long long)P1 << 16) + P2;
-          const long long Lo = ((long long)P3 << 16) + P4;
-          // the top bits of V from its own leading bit: shift H up by k = clz(|H|) - 2, so that
-          // |H << k| < 2^62 and adding the |Lo| part (< 2^48) cannot pass 2^63 (k = 32: V fits in
-          // 64 bits and is kept whole); at least 61 bits are kept, the bits of Lo dropped lie below
-          // 2^-61 of |V|.  They are rounded to a double with integer instructions (a conversion
-          // instruction from 64-bit integers runs on the FP64 pipe, the scarce unit here)
-          const long long aH = H < 0 ? -H : H;
-          const int k = aH ? min(32, __clzll(aH) - 2) : 32;
-          const long long top = (H << k) + (Lo >> (32 - k));
-          double v = i64_to_double(top, e + fcol[n] - 2112 + 32 - k);
-          if (!p.beta_zero) {
-            if (!p.cplx) {
-              v = fma(p.beta[0], cold[x], v);
-            } else {  // (re, im) = (cold[x & ~1], cold[x | 1]); c0 is a multiple of 8
-              const double cr = cold[x & ~1], ci = cold[x | 1];
-              v = (n & 1) ? fma(p.beta[0], ci, fma(p.beta[1], cr, v)) : fma(p.beta[0], cr, fma(-p.beta[1], ci, v));
+            for (int x = 0; x < 8; x++) out[x] = fma(p.beta[0], cold[x], out[x]);
+          } else {
+#pragma unroll
+            for (int x = 0; x < 8; x += 2) {  // (re, im) pairs: c0 is a multiple of 8
+              const double cr = cold[x], ci = cold[x + 1];
+              out[x] = fma(p.beta[0], cr, fma(-p.beta[1], ci, out[x]));
+              out[x + 1] = fma(p.beta[0], ci, fma(p.beta[1], cr, out[x + 1]));
             }
           }
-          out[x] = v;
         }
         if (whole(c0)) {
 #pragma unroll
