@@ -7,8 +7,9 @@
 // Scheme:
 //   * alpha is folded into B once (FP64, one rounding per B element).  Column n of alpha*B gets a
 //     shared exponent f_n; row r of A gets the exponent e_r of its largest element.  Every value
-//     becomes a 62-bit fixed-point integer and 8 balanced base-256 digits (exact in BF16), as in
-//     the split TSMTTSM (split.cu).
+//     becomes a 62-bit fixed-point integer and 8 balanced base-256 digits (exact in FP16), as in
+//     the split TSMTTSM (split.cu); A's digits are formed with byte permutes and one HFMA2 per
+//     digit pair (digit_pairs).
 //   * The MMA contraction runs over (digit, column m).  A' (128 rows x 8*MP) holds A's digit planes
 //     with the least significant first: plane p holds digit 8-p.  B' (N x 8*MP) holds B's planes
 //     with the most significant first: plane q holds digit q+1.  For level L = i+j (2..9) the
@@ -33,7 +34,7 @@
 // Complex FP64 (interleaved) runs as the real product of doubled width: A (K x 2M), B' (2M x 2N)
 // with B'[2n][2m] = br, B'[2n][2m+1] = -bi, B'[2n+1][2m] = bi, B'[2n+1][2m+1] = br, C (K x 2N).
 // Inputs must be finite.
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstring>
 
@@ -76,7 +77,7 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo) {
   d |= (uint64_t)1 << 46;
   return d;
 }
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -102,17 +103,25 @@ __device__ __forceinline__ uint32_t exp_field(double x) {
   return nz ? (ef ? ef : 1u) : 0u;
 }
 
+// G = F + 0x8080...80 for the 62-bit fixed-point magnitude F of x relative to exponent field E:
+// byte i of G (most significant first) is digit i + 128, so the digits are balanced
+__device__ __forceinline__ void g_words(double x, uint32_t E, uint32_t& gh, uint32_t& gl, bool& neg) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t ef = (hi >> 20) & 0x7FF;
+  neg = (hi >> 31) != 0;
+  const uint32_t eff = ef ? ef : 1u;
+  const uint64_t mant = ((uint64_t)((hi & 0xFFFFFu) | (ef ? 0x100000u : 0u)) << 32) | lo;
+  const uint32_t sh = E - eff;
+  const uint64_t F = sh < 64 ? ((mant << 9) >> sh) : 0ull;
+  const uint64_t G = F + 0x8080808080808080ull;
+  gh = (uint32_t)(G >> 32);
+  gl = (uint32_t)G;
+}
+
 // 8 balanced digits of x relative to exponent field E (most significant first), as exact floats
 __device__ __forceinline__ void digits_of(double x, uint32_t E, float (&d)[DIGITS], bool& neg) {
-  uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  uint32_t ef = (hi >> 20) & 0x7FF;
-  neg = (hi >> 31) != 0;
-  uint32_t eff = ef ? ef : 1u;
-  uint64_t mant = ((uint64_t)((hi & 0xFFFFFu) | (ef ? 0x100000u : 0u)) << 32) | lo;
-  uint32_t sh = E - eff;
-  uint64_t F = sh < 64 ? ((mant << 9) >> sh) : 0ull;
-  uint64_t G = F + 0x8080808080808080ull;
-  uint32_t gh = (uint32_t)(G >> 32), gl = (uint32_t)G;
+  uint32_t gh, gl;
+  g_words(x, E, gh, gl, neg);
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     d[i] = __uint_as_float(0x4B000000u | ((gh >> (8 * (3 - i))) & 0xFF)) - 8388736.0f;
@@ -120,10 +129,38 @@ __device__ __forceinline__ void digits_of(double x, uint32_t E, float (&d)[DIGIT
   }
 }
 
+// two FP16 digits (a in the low half), signs applied
 __device__ __forceinline__ uint32_t pack2(float a, float b, bool na, bool nb) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  __half2 h = __floats2half2_rn(a, b);
   uint32_t u = *reinterpret_cast<uint32_t*>(&h);
   return u ^ ((na ? 0x8000u : 0u) | (nb ? 0x80000000u : 0u));
+}
+
+// The eight FP16 digit pairs of elements a, b (a in the low halves), digit i in out[i].  A byte g
+// of G becomes the half 1024 + g by pairing it with the byte 0x64 (two byte permutes), and one
+// HFMA2 subtracts 1152 and applies each element's sign: (1024 + g - 1152) * s = (g - 128) * s,
+// exact in FP16.  About 1.25 instructions per digit.
+__device__ __forceinline__ void digit_pairs(uint32_t gha, uint32_t gla, bool na, uint32_t ghb, uint32_t glb, bool nb,
+                                            uint32_t (&out)[DIGITS]) {
+  const __half2 s = __halves2half2(na ? __float2half(-1.0f) : __float2half(1.0f),
+                                   nb ? __float2half(-1.0f) : __float2half(1.0f));
+  const __half2 c = __hmul2(s, __float2half2_rn(-1152.0f));
+  auto dig = [&](uint32_t pair, uint32_t sel) {
+    const uint32_t u = __byte_perm(pair, 0x64646464u, sel);
+    __half2 h = *reinterpret_cast<const __half2*>(&u);
+    h = __hfma2(h, s, c);
+    return *reinterpret_cast<const uint32_t*>(&h);
+  };
+#pragma unroll
+  for (int w = 0; w < 2; w++) {
+    const uint32_t ga = w ? gla : gha, gb = w ? glb : ghb;
+    const uint32_t x01 = __byte_perm(ga, gb, 0x6273);  // [a.b3, b.b3, a.b2, b.b2]
+    const uint32_t x23 = __byte_perm(ga, gb, 0x4051);  // [a.b1, b.b1, a.b0, b.b0]
+    out[4 * w + 0] = dig(x01, 0x4140);
+    out[4 * w + 1] = dig(x01, 0x4342);
+    out[4 * w + 2] = dig(x23, 0x4140);
+    out[4 * w + 3] = dig(x23, 0x4342);
+  }
 }
 
 // K-major no-swizzle operand: element (row, k) of a tile whose k-octets are lbo bytes apart
@@ -264,7 +301,8 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const
   tc_after();
   const uint32_t tmem = *tslot;
 
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NM >> 3) << 17) | ((128u >> 4) << 24);
+  // kind::f16 with FP16 A and B (a/b format 0), FP32 accumulators, N = NM, M = 128
+  const uint32_t idesc = (1u << 4) | ((uint32_t)(NM >> 3) << 17) | ((128u >> 4) << 24);
   const int row = tid & (ROWS - 1), part = tid >> 7;
   const bool slicer = part < TPS;
   const int m0 = (slicer ? part : 0) * PART;
@@ -400,16 +438,20 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const
           *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) = make_uint4(0, 0, 0, 0);
         continue;
       }
-      float d[8][DIGITS];
-      bool ng[8];
+      uint32_t dp[4][DIGITS];  // element pairs (0,1), (2,3), (4,5), (6,7) of the octet
 #pragma unroll
-      for (int q2 = 0; q2 < 8; q2++) digits_of(v[o * 8 + q2], (uint32_t)e_row, d[q2], ng[q2]);
+      for (int q2 = 0; q2 < 4; q2++) {
+        uint32_t gha, gla, ghb, glb;
+        bool na, nb;
+        g_words(v[o * 8 + 2 * q2], (uint32_t)e_row, gha, gla, na);
+        g_words(v[o * 8 + 2 * q2 + 1], (uint32_t)e_row, ghb, glb, nb);
+        digit_pairs(gha, gla, na, ghb, glb, nb, dp[q2]);
+      }
 #pragma unroll
       for (int pl = 0; pl < DIGITS; pl++) {
         const int i = 7 - pl;  // 0-based digit index held by plane pl
-        uint4 w = make_uint4(pack2(d[0][i], d[1][i], ng[0], ng[1]), pack2(d[2][i], d[3][i], ng[2], ng[3]),
-                             pack2(d[4][i], d[5][i], ng[4], ng[5]), pack2(d[6][i], d[7][i], ng[6], ng[7]));
-        *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) = w;
+        *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) =
+            make_uint4(dp[0][i], dp[1][i], dp[2][i], dp[3][i]);
       }
     }
     if (tid < ROWS) er[tid] = e_row;  // the epilogue of this tile reads er[r]
@@ -446,7 +488,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const
         const int kq = (L - 1) * MP / 16;  // K-steps of 16
         const int ka = (9 - L) * MP / 8;   // first k-octet of A' for this level
         for (int ks = 0; ks < kq; ks++)
-          mma_bf16(dcol + (uint32_t)((L - 2) * NM), make_desc(a0 + (uint32_t)(ka + 2 * ks) * lbo_a, lbo_a),
+          mma_f16(dcol + (uint32_t)((L - 2) * NM), make_desc(a0 + (uint32_t)(ka + 2 * ks) * lbo_a, lbo_a),
                    make_desc(b0 + (uint32_t)(2 * ks) * lbo_b, lbo_b), idesc, ks > 0 ? 1u : 0u);
       }
       mma_commit(&bar_mma[it & 1]);  // one of the four arrivals that complete the tile's phase
@@ -542,7 +584,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   a.inplace = (const void*)A == (const void*)C;
   a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
   a.vecc = ((uintptr_t)C % 16 == 0) && (a.ldc % 2 == 0);
-  a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x bf16
+  a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x fp16
   const int64_t bdig = round_up((int64_t)8 * MP * a.NM * 2, 1024);
   const int64_t avail = h->dev.smem_optin - HDR - bdig;
   a.nabuf = avail >= 2 * (int64_t)a.abuf ? 2 : 1;
