@@ -539,7 +539,7 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       set_error("split precision TSMM: real widths <= 64, or <= 128 out of place");
       return SKINNY_UNSUPPORTED;
     }
-    if (autoselect && (K < 8192 || Nr < 16 || Mr < 8)) {
+    if (autoselect && (K < 8192 || Nr < 8 || Mr < 4 || Mr * Nr < 128)) {
       set_error("split precision TSMM: not selected automatically for this shape");
       return SKINNY_UNSUPPORTED;
     }
@@ -553,12 +553,13 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       }
     return SKINNY_OK;
   }
-  // auto selection (measured on GB300, K with A of 1 GiB, and over every C5 width pair with ~512
-  // MB operands), on the real widths (complex doubled): split wins from Mr * Nr >= 256 with
-  // Nr >= 16 and a contraction width Mr >= 8 (real 8x32 1.4x, 16x16 1.6x, complex 4x16 1.4x,
-  // complex 8x8 1.6x, real 64x64 6x); narrower products stay on the CUDA-core kernels (real 8x8
-  // 0.66x, real 4x64 0.67x, complex 1x64 0.35x, complex 2x32 0.64x).  The autotuner can override.
-  const bool wins = Mr * Nr >= 256 && Nr >= 16 && Mr >= 8;
+  // auto selection (measured on GB300 over every width pair of {1, 2, 4, 8, 16, 32, 64}^2, FP64
+  // and complex FP64, ~512 MB of operands), on the real widths (complex doubled): split wins from
+  // Mr * Nr >= 128 with Nr >= 8 and a contraction width Mr >= 4 (real 8x16 1.5x, 16x8 1.4x, 4x32
+  // 1.2x, 64x8 1.7x, 64x64 9.8x; complex 4x8 1.5x, 32x4 1.65x, 64x64 7.3x); narrower products stay
+  // on the CUDA-core kernels (real 8x8 0.83x, 4x16 0.82x, 32x4 0.68x, complex 1x64 0.65x).  The
+  // autotuner can override.
+  const bool wins = Mr * Nr >= 128 && Nr >= 8 && Mr >= 4;
   if (autoselect && (K < 8192 || !wins)) {
     set_error("split precision TSMM: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
