@@ -1006,7 +1006,11 @@ def run_precision(args):
 
 def measure_e2e(h, items, ops, args, world):
     """Same metric through the public API with HOST buffers: every step copies each shape's inputs
-    from pinned host memory to the device, runs the product and copies the result back."""
+    from pinned host memory to the device, runs the product and copies the result back to pinned
+    host memory.  The shapes are pipelined as a caller streaming many products would: uploads on
+    one stream, products on a second (each waits for its own upload), downloads on a third (each
+    waits for its own product), so one shape's upload overlaps the previous shape's product and
+    download (the two copy directions run on separate copy engines)."""
     import torch
     maxA = max(o["A"][0].numel() * o["A"][0].element_size() for o in ops)
     maxB = max(o["B"][0].numel() * o["B"][0].element_size() for o in ops)
@@ -1014,46 +1018,69 @@ def measure_e2e(h, items, ops, args, world):
     hA = torch.empty(maxA, dtype=torch.uint8, pin_memory=True)
     hB = torch.empty(maxB, dtype=torch.uint8, pin_memory=True)
     hC = torch.empty(maxC, dtype=torch.uint8, pin_memory=True)
+    hOut = torch.empty(maxC, dtype=torch.uint8, pin_memory=True)  # downloads never race uploads
     # host values must be finite numbers: fill as uniform doubles
-    for t in (hA, hB, hC):
+    for t in (hA, hB, hC, hOut):
         d = t.view(torch.float64)
         d.uniform_(-1, 1)
     steps = max(1, min(args.steps, 3))
+    s_in, s_cmp, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
 
     def as_bytes(t):
         return (torch.view_as_real(t) if t.is_complex() else t).view(torch.uint8)
 
     h2d = d2h = 0
+    prev_out = [None] * len(items)  # a shape's download in the previous step
 
     def one():
         nonlocal h2d, d2h
         h2d = d2h = 0
-        for it, op in zip(items, ops):
+        for i, (it, op) in enumerate(zip(items, ops)):
             A, B, C = op["A"][0], op["B"][0], op["C"]
             nA, nB, nC = (x.numel() * x.element_size() for x in (A, B, C))
-            as_bytes(A).view(-1).copy_(hA[:nA], non_blocking=True)
-            as_bytes(B).view(-1).copy_(hB[:nB], non_blocking=True)
-            h2d += nA + nB
-            if it["op"] == "tsmm" and not it["inplace"]:
-                as_bytes(C).view(-1).copy_(hC[:nC], non_blocking=True)
-                h2d += nC
-            call(h, it, op, 0, args.method)
-            hC[:nC].copy_(as_bytes(C).view(-1), non_blocking=True)
-            d2h += nC
-    one()
+            up, done, out = torch.cuda.Event(), torch.cuda.Event(), torch.cuda.Event()
+            if prev_out[i] is not None:  # this shape's buffers are free once its last download ran
+                s_in.wait_event(prev_out[i])
+            with torch.cuda.stream(s_in):
+                as_bytes(A).view(-1).copy_(hA[:nA], non_blocking=True)
+                as_bytes(B).view(-1).copy_(hB[:nB], non_blocking=True)
+                h2d += nA + nB
+                if it["op"] == "tsmm" and not it["inplace"]:
+                    as_bytes(C).view(-1).copy_(hC[:nC], non_blocking=True)
+                    h2d += nC
+                up.record(s_in)
+            s_cmp.wait_event(up)
+            with torch.cuda.stream(s_cmp):
+                call(h, it, op, 0, args.method)
+                done.record(s_cmp)
+            s_out.wait_event(done)
+            with torch.cuda.stream(s_out):
+                hOut[:nC].copy_(as_bytes(C).view(-1), non_blocking=True)
+                d2h += nC
+                out.record(s_out)
+            prev_out[i] = out
+
+    def run(n):
+        cur = torch.cuda.current_stream()
+        for st in (s_in, s_cmp, s_out):
+            st.wait_stream(cur)
+        for _ in range(n):
+            one()
+        for st in (s_in, s_cmp, s_out):
+            cur.wait_stream(st)
+
+    run(1)
     torch.cuda.synchronize()
     barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    for _ in range(steps):
-        one()
+    run(steps)
     e1.record()
     torch.cuda.synchronize()
     ms = max_over_ranks(e0.elapsed_time(e1), world)
     b = sum_over_ranks(sum(it["bytes"] for it in items) * steps, world)
     return {"value": round(b / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "steps": steps}
-
+            "d2h_bytes_per_step": int(d2h), "steps": steps, "pipeline": "upload / product / download streams"}
 
 if __name__ == "__main__":
     main()
