@@ -2,7 +2,7 @@
 // counterpart in the reference, whose FP64 kernels are CUDA-core DFMA loops, e.g.
 // tsmttsm/genv5.cuh:28-89).  Wider products go to split_wide.cu.
 //
-// Why: GB300 executes 595 G FP64 FMA/s but 2.25 P BF16 tensor flop/s.  A CUDA-core FP64 TSMTTSM
+// Why: GB300 executes 595 G FP64 FMA/s but 2.25 P FP16 / BF16 tensor flop/s.  A CUDA-core FP64 TSMTTSM
 // is FP64-bound for every M = N >= 2.  Here each FP64 product is computed exactly from 8-bit
 // pieces on the tensor cores, and FP64 arithmetic is used only a few times per 1024 rows.
 //
@@ -11,9 +11,9 @@
 //     seen in the current accumulation period.  Each element x is written as a 62-bit fixed-point
 //     integer F = |x| * 2^(1084 - E) (< 2^62) and F as 8 balanced base-256 digits
 //     d_1..d_8 in [-128, 128] (d_1 most significant): x = sign * sum_i d_i 2^(8(8-i)) 2^(E-1084).
-//     Digits are exact in BF16.
+//     Digits are exact in FP16 (formed with byte permutes, digits.cuh).
 //   * Digit planes are stacked along the MMA dimensions: A rows (i-1)*MP + m, B rows
-//     (j-1)*NP + n, so one tcgen05.mma (M = 128, N = 8*NP, K = 16, BF16 x BF16 -> FP32 in TMEM)
+//     (j-1)*NP + n, so one tcgen05.mma (M = 128, N = 8*NP, K = 16, FP16 x FP16 -> FP32 in TMEM)
 //     forms every digit-pair product d_i(a) d_j(b) for 16 rows of K.
 //   * |d_i d_j| <= 2^14, so over a period of <= 1024 rows every partial sum is an integer of
 //     magnitude <= 2^24: the FP32 accumulation in TMEM is exact.  A period ends after 1024 rows,
@@ -28,11 +28,11 @@
 //   * Cross-CTA finish as in the CUDA-core kernel: CTA partials in FP64, the last CTA (ticket)
 //     sums them in CTA order, applies alpha/beta.
 // Inputs must be finite (Inf/NaN have no fixed-point form).
-#include <cuda_bf16.h>
 
 #include <cstring>
 
 #include "api_internal.h"
+#include "digits.cuh"
 
 namespace skinny {
 
@@ -76,7 +76,7 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo) {
   return d;                                    // no swizzle
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -122,51 +122,30 @@ __device__ __forceinline__ uint32_t exp_field(double x) {
   return nz ? (ef ? ef : 1u) : 0u;
 }
 
-// 8 balanced digits of x relative to exponent field E, as float values (exact integers)
-__device__ __forceinline__ void digits_of(double x, uint32_t E, float (&d)[DIGITS], bool& neg) {
-  uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  uint32_t ef = (hi >> 20) & 0x7FF;
-  neg = (hi >> 31) != 0;
-  uint32_t eff = ef ? ef : 1u;
-  uint64_t mant = ((uint64_t)((hi & 0xFFFFFu) | (ef ? 0x100000u : 0u)) << 32) | lo;
-  uint32_t sh = E - eff;  // E >= eff for every element of the period
-  uint64_t F = sh < 64 ? ((mant << 9) >> sh) : 0ull;
-  uint64_t G = F + 0x8080808080808080ull;
-  uint32_t gh = (uint32_t)(G >> 32), gl = (uint32_t)G;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    uint32_t bh = (gh >> (8 * (3 - i))) & 0xFF;
-    uint32_t bl = (gl >> (8 * (3 - i))) & 0xFF;
-    d[i] = __uint_as_float(0x4B000000u | bh) - 8388736.0f;      // byte - 128, exact
-    d[4 + i] = __uint_as_float(0x4B000000u | bl) - 8388736.0f;
-  }
-}
-
 __device__ __forceinline__ double pow2i(int e) {  // 2^e for e in [-1022, 1023], clamped outside
   e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
   return __hiloint2double((e + 1023) << 20, 0);
 }
 
 // Slice one unit: 8 consecutive rows (octet o) of column c into the digit buffer `buf`
-// (rows (i-1)*CP + c), relative to exponent E.
+// (rows (i-1)*CP + c), relative to exponent E.  FP16 digits formed from the bytes of G with byte
+// permutes and one HFMA2 per digit pair (digits.cuh).
 __device__ __forceinline__ void slice_unit(const double (&v)[8], uint32_t E, int c, int CP, int o,
                                            uint32_t lbo, unsigned char* buf) {
-  float d[8][DIGITS];
-  bool ng[8];
+  uint32_t dp[4][NDIGITS];  // row pairs (0,1), (2,3), (4,5), (6,7) of the octet
 #pragma unroll
-  for (int q = 0; q < 8; q++) digits_of(v[q], E, d[q], ng[q]);
+  for (int q = 0; q < 4; q++) {
+    uint32_t gha, gla, ghb, glb;
+    bool na, nb;
+    g_words(v[2 * q], E, gha, gla, na);
+    g_words(v[2 * q + 1], E, ghb, glb, nb);
+    digit_pairs(gha, gla, na, ghb, glb, nb, dp[q]);
+  }
 #pragma unroll
   for (int i = 0; i < DIGITS; i++) {
-    uint32_t w[4];
-#pragma unroll
-    for (int p = 0; p < 4; p++) {
-      __nv_bfloat162 h = __floats2bfloat162_rn(d[2 * p][i], d[2 * p + 1][i]);
-      uint32_t u = *reinterpret_cast<uint32_t*>(&h);
-      u ^= (ng[2 * p] ? 0x8000u : 0u) | (ng[2 * p + 1] ? 0x80000000u : 0u);
-      w[p] = u;
-    }
     const int r = i * CP + c;
-    *reinterpret_cast<uint4*>(buf + o * lbo + (r >> 3) * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(buf + o * lbo + (r >> 3) * 128 + (r & 7) * 16) =
+        make_uint4(dp[0][i], dp[1][i], dp[2][i], dp[3][i]);
   }
 }
 
@@ -229,8 +208,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
     for (int i = 0; i < nt && i < p.stages; i++)
       if (is_bulk(t_begin + i)) issue(t_begin + i, i);
 
-  // idesc: D f32, A/B bf16, K-major both, N = nmma, M = 128
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(p.nmma >> 3) << 17) | ((128u >> 4) << 24);
+  // idesc: D f32, A/B f16, K-major both, N = nmma, M = 128
+  const uint32_t idesc = (1u << 4) | ((uint32_t)(p.nmma >> 3) << 17) | ((128u >> 4) << 24);
 
   // Slicing units: (operand, column c, k-octet o).  A units u < nA: c = u % MP, o = u / MP;
   // B units nA <= u < nA + nB: c = (u - nA) % NP.  nA is a multiple of 32, so a warp holds units
@@ -414,7 +393,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
       const uint32_t lbb = p.gram ? p.lbo_a : p.lbo_b;
       const int ksteps = RSW / 16;
       for (int ks = 0; ks < ksteps; ks++)
-        mma_bf16(tmem, make_desc(a0 + 2 * ks * p.lbo_a, p.lbo_a), make_desc(b0 + 2 * ks * lbb, lbb), idesc,
+        mma_f16(tmem, make_desc(a0 + 2 * ks * p.lbo_a, p.lbo_a), make_desc(b0 + 2 * ks * lbb, lbb), idesc,
                  (period_rows > 0 || ks > 0) ? 1u : 0u);
       mma_commit(&bar_mma[b]);
       if (p.bulk && it + p.stages < nt && is_bulk(t + p.stages)) {
