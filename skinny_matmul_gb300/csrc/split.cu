@@ -482,10 +482,10 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
     set_error("split precision TSMTTSM: M, N <= 128");
     return SKINNY_UNSUPPORTED;
   }
-  // auto selection (measured on GB300): the split kernel wins from M*N >= 256 on, and from
-  // M*N >= 128 when both widths are at least 8 (8x16 1.18x, 16x8 1.29x; complex 4x8 and 8x4 through
-  // the real product 1.1-1.2x); below that the CUDA-core FP64 kernel is as fast or faster (8x8
-  // 0.97x, 4x32 0.44x).  The wide kernel costs about as much per 64 x 64
+  // auto selection (measured on GB300): the split kernel wins from M*N >= 256 on, and whenever
+  // both widths are at least 8 (8x8 1.07x at 512 MB of operands and 1.29x at K = 2^20, 8x16 1.37x,
+  // 16x8 1.44x; complex 4x8 and 8x4 through the real product 1.3x); below that the CUDA-core FP64
+  // kernel is as fast or faster (4x16 0.71x, 4x32 0.44x).  The wide kernel costs about as much per 64 x 64
   // block whatever the block's fill (12.5 ms per block at K = 2^24; CUDA-core FP64 takes 23 ms at
   // M = N = 17 and 114 ms at 64), so it is chosen from M*N >= 320 per block on.  The autotuner can
   // override per shape.
@@ -493,7 +493,7 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   const int64_t sym_w = (A == B && lda == ldb && M == N) ? 1 : 0;
   const int64_t bm = (M + 63) / 64, bn = (N + 63) / 64;
   const int64_t nblk_w = sym_w ? bm * (bm + 1) / 2 : bm * bn;
-  const bool narrow_wins = M * N >= 256 || (M * N >= 128 && M >= 8 && N >= 8);
+  const bool narrow_wins = M * N >= 256 || (M >= 8 && N >= 8);
   if (autoselect && (K < 4096 || !narrow_wins || (wide && M * N < 320 * nblk_w))) {
     set_error("split precision: not selected automatically for this shape");
     return SKINNY_UNSUPPORTED;
