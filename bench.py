@@ -242,6 +242,27 @@ def make_operands(it, device, seed):
                 C=torch.zeros(M * N, dtype=tdt, device=device))
 
 
+def kernel_of(it, method):
+    """The kernel family a shape runs on under `method`, by the library's selection rules (the ncu
+    launch lists in profiles/ confirm them)."""
+    M, N, K = it["M"], it["N"], it["K"]
+    fp64 = it["dt"] in ("f64", "c64")
+    if it["op"] == "tsmttsm":
+        Mr, Nr = (2 * M, 2 * N) if it["dt"] == "c64" else (M, N)
+        wide = Mr > 16 or Nr > 16
+        nblk = ((Mr + 63) // 64) * ((Nr + 63) // 64)
+        auto_split = K >= 4096 and (Mr * Nr >= 256 or (Mr >= 8 and Nr >= 8)) and \
+            (not wide or Mr * Nr >= 320 * nblk)
+        if fp64 and (method == "split" or (method == "auto" and auto_split)):
+            return "split_wide_kernel" if wide else "split_tsmttsm_kernel"
+        return "tsmttsm_kernel"
+    Mr, Nr = (2 * M, 2 * N) if it["dt"] == "c64" else (M, N)
+    auto_split = K >= 8192 and Mr * Nr >= 128 and Nr >= 8 and Mr >= 4
+    if fp64 and (method == "split" or (method == "auto" and auto_split)):
+        return "split_tsmm_kernel"
+    return "tsmm_kernel"
+
+
 def call(h, it, ops, i, method):
     M, N, K = it["M"], it["N"], it["K"]
     # FP64 and complex FP64 take the method (split covers complex TSMM); dd is real FP64 only
@@ -439,10 +460,13 @@ def main():
     # per-shape table and the dominant kernel's roofline (sum over its launches)
     per = []
     kern_ms = 0.0
+    by_kernel = {}
     for j, it in enumerate(items):
         ts = sorted(ev[i][j][0].elapsed_time(ev[i][j][1]) for i in range(args.steps))
         t = ts[len(ts) // 2] * 1e-3
         kern_ms += sum(ev[i][j][0].elapsed_time(ev[i][j][1]) for i in range(args.steps))
+        kname = kernel_of(it, args.method)
+        by_kernel[kname] = by_kernel.get(kname, 0.0) + t
         gbs = it["bytes"] / t / 1e9
         tf = it["flops"] / t / 1e12
         per.append({"op": it["op"], "dtype": it["dt"], "M": it["M"], "N": it["N"], "K": it["K"],
@@ -453,7 +477,8 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get(args.workload),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "kernel": "tsmm_kernel" if items[0]["op"] == "tsmm" else "tsmttsm_kernel",
+                "kernel": max(by_kernel, key=by_kernel.get),
+                "kernel_time_shares": {k: round(v / sum(by_kernel.values()), 3) for k, v in by_kernel.items()},
                 "fp64_tflops": round(flops_step * args.steps / (kern_ms * 1e-3) / 1e12, 3),
                 "fp64_peak_tflops_measured": FP64_PEAK_TFLOPS}
 
