@@ -52,6 +52,23 @@ def test_bad_arguments_rejected_without_device(skinny_lib):
     assert r == 0
 
 
+def test_group_and_grouping_arguments_rejected_without_device(skinny_lib):
+    """skinny_group with no handle or a negative count, and set_grouping with a bad group size or
+    no server, fail with SKINNY_BAD_ARG before any device work; a dry server accepts a valid
+    grouping configuration."""
+    from skinny_matmul_gb300 import lib as L
+    from skinny_matmul_gb300.api import Server
+    items = (L.GroupItem * 1)()
+    assert skinny_lib.skinny_group(None, L.R64, items, 1, None) == L.BAD_ARG
+    assert skinny_lib.skinny_group(None, L.R64, items, -1, None) == L.BAD_ARG
+    assert skinny_lib.skinny_server_set_grouping(None, 1 << 20, 16) == L.BAD_ARG
+    s = Server(None, 1 << 30)
+    assert skinny_lib.skinny_server_set_grouping(s.s, 1 << 20, 0) == L.BAD_ARG
+    assert skinny_lib.skinny_server_set_grouping(s.s, 1 << 20, 70000) == L.BAD_ARG
+    assert skinny_lib.skinny_server_set_grouping(s.s, 0, 1) == L.OK  # grouping off
+    s.close()
+
+
 def test_launcher_list_shape():
     from skinny_matmul_gb300 import launchers
     for op in ("tsmttsm", "tsmm"):
