@@ -333,12 +333,18 @@ def barrier(world):
         dist.barrier()
 
 
+def _reduce_device():
+    """Where a reduction's tensor lives: the GPU under NCCL, the host under gloo (the CPU tests)."""
+    import torch.distributed as dist
+    return "cpu" if dist.get_backend() == "gloo" else "cuda"
+
+
 def max_over_ranks(v, world):
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -348,7 +354,7 @@ def sum_over_ranks(v, world):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
