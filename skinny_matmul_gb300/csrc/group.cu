@@ -25,6 +25,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "api_internal.h"
 #include "group.h"
@@ -356,7 +357,7 @@ int ilog2(int v) {
 }  // namespace
 
 void* group_kernel_fn(int cls) {
-  static bool attr[GROUP_CLASSES] = {false, false, false, false};
+  static std::once_flag attr[GROUP_CLASSES];  // the shared-memory attribute, once per class and process
   void* fn = nullptr;
   switch (cls) {
     case SKINNY_R32: fn = (void*)group_kernel<float, float>; break;
@@ -365,10 +366,7 @@ void* group_kernel_fn(int cls) {
     case SKINNY_C64: fn = (void*)group_kernel<c64, c64>; break;
     default: return nullptr;
   }
-  if (!attr[cls]) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, GROUP_SMEM);
-    attr[cls] = true;
-  }
+  std::call_once(attr[cls], [fn] { cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, GROUP_SMEM); });
   return fn;
 }
 
