@@ -2,7 +2,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls this code;
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm use it,
- * and only as the checker (or as the timed CPU implementation of the reference's loops).
+ * and only as the reference results the GPU path is compared with (or as the timed CPU
+ * implementation of the reference's loops).
  *
  * Three families:
  *   orc_tsmttsm_* / orc_tsmm_*   plain loops in the working type, OpenMP-parallel in the

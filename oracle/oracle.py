@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline / reference arm, never by the product package.  It is the checker, not the thing
-measured or shipped.
+baseline / reference arm, never by the product package.  It supplies the results the GPU path is compared with; it
+is not the thing measured or shipped.
 
 Every function takes flat numpy storage buffers plus (M, N, K, ld*) in the reference's layout
 (versions.hpp:43-45):
