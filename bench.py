@@ -560,8 +560,7 @@ TRAFFIC = {}
 # family's launches differ in size, so one per-launch figure of the step does not exist).
 PROBE_TRAFFIC = {
     "tsmm-sweep": {"kernel": "split_tsmm_kernel<64, 512>", "shape": "FP64 TSMM 64 x 64, K = 2^20, beta 0.5",
-                   "dram_bytes": 1074e6 + 487e6, "algorithmic_bytes": 1611e6,
-                   "summary": "profiles/split_tsmm_kernel_f64_64x64_K1M.md"},
+                   "dram_bytes": 1074e6 + 487e6, "algorithmic_bytes": 1611e6},
 }
 
 
