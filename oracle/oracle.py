@@ -26,9 +26,18 @@ _SUFFIX = {np.dtype(np.float32): "s", np.dtype(np.float64): "d",
            np.dtype(np.complex64): "c", np.dtype(np.complex128): "z"}
 
 
+# Where the reference tree is mounted when the reference's own kernels are compiled (the cubins
+# in oracle/_ref are built only where it exists and are used as prebuilt files elsewhere).
+REFERENCE_TREE = os.environ.get("SKINNY_REFERENCE_TREE", "/root/reference")
+
+
 def build() -> str:
-    """Compile the oracle with its Makefile (gcc + OpenMP); returns the library path."""
+    """Compile the oracle with its Makefile (gcc + OpenMP) and the runner of the reference's
+    kernels; where the reference tree exists, also the reference's kernels (oracle/_ref).
+    Returns the oracle library's path."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    if os.path.isdir(os.path.join(REFERENCE_TREE, "tsmttsm")):
+        subprocess.run(["make", "-s", "-j5", "-C", _HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
     return _LIB_PATH
 
 
