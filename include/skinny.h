@@ -80,6 +80,13 @@ const char* skinny_last_error(void);
 /* Synchronises the device and reports SKINNY_TIMEOUT if a kernel's bounded wait gave up since
  * the last check (the flag is then cleared and the handle's workspaces are reset). */
 skinny_status skinny_check_device(skinny_handle handle);
+/* Poll limit of the CUDA-core TSMTTSM kernel's bounded waits on its copy ring (default
+ * 4194304 polls, each suspending for a hardware-chosen interval: well above a second).  A wait
+ * that runs out records a timeout for skinny_check_device; its CTA first waits, with the default
+ * bound, for the copies it has already issued, then exits without writing C.  0 makes every such
+ * wait give up at once, which exercises that path without a fault.  No counterpart in the
+ * reference (its kernels have no waits that can time out). */
+skinny_status skinny_set_wait_limit(skinny_handle handle, uint32_t polls);
 
 /* Number of kernels this library has launched in this process (all devices, all handles);
  * lets a caller count device launches inside a timed region.  No counterpart in the reference. */
@@ -142,13 +149,21 @@ skinny_status skinny_svqb_z(skinny_handle handle, skinny_acc gram_acc, int64_t K
  * still the caller's.  It uses the current device and the given stream.
  *   - The first call on a device looks up the array's device address; make it before any stream
  *     capture.
- *   - M*N*8 bytes of partial sums per CTA must fit in 16 MiB: M*N <= 2097152, else
- *     SKINNY_BAD_ARG; for large M*N the grid is reduced so the partials fit.
- *   - Every call shares the one array (the counters are cleared on the stream at each call):
- *     calls that overlap on the GPU race and must be ordered by the caller. */
+ *   - M*N <= 1048576 (2^20, the most the CUDA-core kernel's reduction handles in FP64), else
+ *     SKINNY_BAD_ARG before any device work; within that, shapes whose row tile does not fit in
+ *     shared memory (M + N above about 1800 when A != B) return SKINNY_UNSUPPORTED, as in
+ *     skinny_tsmttsm.  For large M*N the grid is reduced so the partials fit in the array.
+ *   - Every call shares the one array (its ticket counters are cleared on the stream at each
+ *     call): calls that overlap on the GPU race and must be ordered by the caller.
+ *   - A bounded device-side wait that times out leaves C unwritten; it is reported by
+ *     skinny_tsmttsm_d_static_check, not by this call (which returns before the kernel runs). */
 skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K, const double* A,
                                       int64_t lda, double alpha, const double* B, int64_t ldb,
                                       double beta, double* C, int64_t ldc, void* stream);
+/* Status of the skinny_tsmttsm_d_static calls on the current device: synchronises `stream`, then
+ * returns SKINNY_TIMEOUT (and clears the flag) if a bounded wait of any call since the last check
+ * timed out, else SKINNY_OK.  Allocates nothing. */
+skinny_status skinny_tsmttsm_d_static_check(void* stream);
 
 /* Autotuner.  Replaces the reference's compile-time choice of one kernel variant per (M, N)
  * (versions.hpp:48-177, multi_dispatch.cuh, tsmm/fix_blend.cuh:7-29): for (op, dtype, acc, M, N)

@@ -75,6 +75,10 @@ class Handle:
     def check_device(self):
         return L.check(self.lib.skinny_check_device(self.h))
 
+    def set_wait_limit(self, polls: int):
+        """Poll limit of the bounded device-side waits (include/skinny.h skinny_set_wait_limit)."""
+        return L.check(self.lib.skinny_set_wait_limit(self.h, polls))
+
     def _product(self, fn, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc, stream, dtype):
         code = dtype if dtype is not None else _dtype_code(A if not isinstance(A, int) else C)
         al, be = _scalar(alpha, code), _scalar(beta, code)

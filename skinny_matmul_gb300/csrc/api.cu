@@ -166,6 +166,13 @@ extern "C" skinny_status skinny_check_device(skinny_handle h) {
   return SKINNY_TIMEOUT;
 }
 
+extern "C" skinny_status skinny_set_wait_limit(skinny_handle h, uint32_t polls) {
+  if (!h) return SKINNY_BAD_ARG;
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->dev.wait_polls = polls;
+  return SKINNY_OK;
+}
+
 // ---------------------------------------------------------------------------------- products
 namespace skinny {
 

@@ -208,10 +208,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: returns false (and records a timeout in *err) after max_iter polls.
-// try_wait itself suspends for a hardware-chosen interval, so 2^22 polls is well above a second.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
-  for (uint32_t i = 0; i < (1u << 22); i++)
+// Default poll limit of a bounded wait.  try_wait itself suspends for a hardware-chosen interval,
+// so 2^22 polls is well above a second.
+constexpr uint32_t kWaitPolls = 1u << 22;
+// Bounded wait: returns false (and records a timeout in *err) after `polls` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err,
+                                                  uint32_t polls = kWaitPolls) {
+  for (uint32_t i = 0; i < polls; i++)
     if (mbar_try_wait(bar, parity)) return true;
   if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
   return false;

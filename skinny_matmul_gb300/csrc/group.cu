@@ -377,7 +377,7 @@ int ilog2(int v) {
 }  // namespace
 
 void* group_kernel_fn(int cls) {
-  static std::once_flag attr[GROUP_CLASSES];  // the shared-memory attribute, once per class and process
+  static SmemAttr attr[GROUP_CLASSES];  // the shared-memory attribute, per class and device
   void* fn = nullptr;
   switch (cls) {
     case SKINNY_R32: fn = (void*)group_kernel<float, float>; break;
@@ -386,7 +386,7 @@ void* group_kernel_fn(int cls) {
     case SKINNY_C64: fn = (void*)group_kernel<c64, c64>; break;
     default: return nullptr;
   }
-  std::call_once(attr[cls], [fn] { cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, GROUP_SMEM); });
+  if (!ensure_smem_attr(fn, GROUP_SMEM, attr[cls])) return nullptr;
   return fn;
 }
 
@@ -591,6 +591,7 @@ extern "C" skinny_status skinny_group(skinny_handle h, skinny_dtype dtype, const
     return SKINNY_DEVICE_ERROR;
   }
   void* fn = group_kernel_fn(dtype);
+  if (!fn) return SKINNY_DEVICE_ERROR;
   const unsigned char* b = ws.batch;
   int cls = (int)dtype;
   void* args[] = {(void*)&b, (void*)&cls, (void*)&ws.part, (void*)&ws.counters};

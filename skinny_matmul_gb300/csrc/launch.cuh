@@ -20,6 +20,7 @@ struct DeviceInfo {
   int id = 0;
   int sms = 0;
   int smem_optin = 0;
+  uint32_t wait_polls = kWaitPolls;  // poll limit of the CUDA-core TSMTTSM's bounded waits
 };
 
 // Per-(handle, stream) workspace: CTA partials + ticket counter for the in-launch reduction.
@@ -50,19 +51,39 @@ inline int pow2ceil(int64_t v) {
 }
 inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
+// The dynamic shared-memory attribute a kernel has been given, per device (the attribute is set
+// per device: cudaFuncSetAttribute acts on the current one).  Zero-initialised as a static.
+constexpr int kMaxDevices = 64;
+struct SmemAttr {
+  std::atomic<int> bytes[kMaxDevices];
+};
+
+// Raises `kernel`'s dynamic shared-memory limit on the current device to at least `bytes`;
+// records only a successful call.  Returns false if the attribute could not be set.
 template <typename K>
-inline void ensure_smem_attr(K kernel, int bytes, std::atomic<int>& done) {
-  if (done.load(std::memory_order_relaxed) >= bytes) return;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  int cur = done.load();
-  while (cur < bytes && !done.compare_exchange_weak(cur, bytes)) {
+inline bool ensure_smem_attr(K kernel, int bytes, SmemAttr& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
   }
+  std::atomic<int>& d = done.bytes[dev];
+  if (d.load(std::memory_order_relaxed) >= bytes) return true;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaFuncSetAttribute(MaxDynamicSharedMemorySize) failed");
+    return false;
+  }
+  int cur = d.load();
+  while (cur < bytes && !d.compare_exchange_weak(cur, bytes)) {
+  }
+  return true;
 }
 
 // ----------------------------------------------------------------------------------- TSMTTSM
 template <typename T, typename Acc, int TM, int TN>
 skinny_status tsmttsm_launch_tile(const TsmttsmArgs<T>& a, dim3 grid, int smem, cudaStream_t st) {
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   auto kern = tsmttsm_kernel<T, Acc, TM, TN>;
   ensure_smem_attr(kern, smem, attr);
   kern<<<grid, TSMTTSM_THREADS, smem, st>>>(a);
@@ -200,13 +221,14 @@ skinny_status tsmttsm_run(const DeviceInfo& dev, Workspace& ws, int* err, cudaSt
   a.partials = ws.partials;
   a.counter = ws.counter;
   a.err = err;
+  a.polls = dev.wait_polls;
   return tsmttsm_dispatch<T, Acc>(pl.tm, pl.tn, a, dim3(pl.grid, pl.groups), pl.smem, st);
 }
 
 // -------------------------------------------------------------------------------------- TSMM
 template <typename T, typename Acc, int TN, int U>
 skinny_status tsmm_launch_tile(const TsmmArgs<T>& a, int bps, int sms, int smem, cudaStream_t st) {
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   auto kern = tsmm_kernel<T, Acc, TN, U>;
   ensure_smem_attr(kern, smem, attr);
   int occ = 1;

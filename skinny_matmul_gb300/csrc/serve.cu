@@ -325,6 +325,7 @@ bool skinny_server_st::slot_prepare(LaneSlot& sl, size_t batch_bytes, size_t par
     cudaKernelNodeParams kp;
     std::memset(&kp, 0, sizeof kp);
     kp.func = group_kernel_fn(c);
+    if (!kp.func) return false;
     kp.gridDim = dim3(group_grid(h->dev.sms));
     kp.blockDim = dim3(GROUP_THREADS);
     kp.sharedMemBytes = GROUP_SMEM;

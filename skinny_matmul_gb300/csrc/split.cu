@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
 
 template <int NP>
 static skinny_status launch(const Args& a, int grid, int smem, cudaStream_t st) {
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   auto kern = split_tsmttsm_kernel<NP>;
   ensure_smem_attr(kern, smem, attr);
   kern<<<grid, THREADS, smem, st>>>(a);

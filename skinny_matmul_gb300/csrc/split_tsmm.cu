@@ -568,23 +568,23 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   switch (MP) {
     case 16:
       if (two) {
-        static std::atomic<int> attr{0};
+        static SmemAttr attr;
         ensure_smem_attr(split_tsmm_kernel<16, 256>, smem, attr);
         split_tsmm_kernel<16, 256><<<(int)grid, 256, smem, st>>>(a);
       } else {
-        static std::atomic<int> attr{0};
+        static SmemAttr attr;
         ensure_smem_attr(split_tsmm_kernel<16, 512>, smem, attr);
         split_tsmm_kernel<16, 512><<<(int)grid, 512, smem, st>>>(a);
       }
       break;
     case 32: {
-      static std::atomic<int> attr{0};
+      static SmemAttr attr;
       ensure_smem_attr(split_tsmm_kernel<32, 512>, smem, attr);
       split_tsmm_kernel<32, 512><<<(int)grid, 512, smem, st>>>(a);
       break;
     }
     default: {
-      static std::atomic<int> attr{0};
+      static SmemAttr attr;
       ensure_smem_attr(split_tsmm_kernel<64, 512>, smem, attr);
       split_tsmm_kernel<64, 512><<<(int)grid, 512, smem, st>>>(a);
       break;

@@ -660,7 +660,7 @@ skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;
   a.err = h->err;
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   ensure_smem_attr(split_wide_kernel, smem, attr);
   split_wide_kernel<<<(int)grid, THREADS, smem, st>>>(a);
   count_launch();

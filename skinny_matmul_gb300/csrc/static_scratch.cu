@@ -8,9 +8,10 @@
 // Host code never passes the array's name to a kernel (in host code it is only a stand-in for
 // the symbol); the first call on each device, with that device current, looks up the device
 // address with cudaGetSymbolAddress and caches it.  Make that first call before any stream
-// capture.  All calls share the one array: the header (ticket counters, error word) is cleared
-// on the stream at every call, and calls that overlap on the GPU (different streams, or host
-// threads racing) use the same partial buffer and race.
+// capture.  All calls share the one array: the ticket counters are cleared on the stream at every
+// call, and calls that overlap on the GPU (different streams, or host threads racing) use the
+// same partial buffer and race.  The error word is left alone by the calls: a bounded wait that
+// timed out sets it, and skinny_tsmttsm_d_static_check() reads and clears it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -26,8 +27,14 @@ extern template skinny_status tsmttsm_plan<double, double>(const DeviceInfo&, in
 extern template skinny_status tsmttsm_dispatch<double, double>(int, int, const TsmttsmArgs<double>&,
                                                                dim3, int, cudaStream_t);
 
-constexpr size_t kStaticHeaderBytes = 512;             // 64 ticket counters + error word at 256
+constexpr size_t kStaticCounterBytes = 256;            // 64 ticket counters, cleared per call
+constexpr size_t kStaticErrOffset = 256;               // device error word (bounded waits)
+constexpr size_t kStaticHeaderBytes = 512;
 constexpr size_t kStaticPartialBytes = (size_t)16 << 20;  // CTA partials: grid * M * N doubles
+// Largest M * N: the CUDA-core kernel reduces through at most 64 groups of 256 cells of 8 x 8
+// entries in FP64 (tsmttsm_plan), i.e. 2^20 entries of C; 2^20 * 8 bytes fills half the array,
+// so at least two CTAs share the rows at the limit.
+constexpr int64_t kStaticMaxCells = (int64_t)1 << 20;
 
 static __device__ __align__(256) unsigned char g_tsmttsm_scratch[kStaticHeaderBytes + kStaticPartialBytes];
 
@@ -78,11 +85,11 @@ extern "C" skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K
   skinny_status s = check_args(false, SKINNY_R64, M, N, K, A, lda, &alpha, B, ldb, &beta, C, ldc);
   if (s != SKINNY_OK) return s;
   if (M == 0 || N == 0) return SKINNY_OK;
-  const size_t per_cta = (size_t)M * (size_t)N * sizeof(double);
-  if (per_cta > kStaticPartialBytes) {
-    set_error("static TSMTTSM: M*N exceeds the static scratch (at most 2097152 entries of C)");
+  if (M * N > kStaticMaxCells) {
+    set_error("static TSMTTSM: M*N exceeds the static scratch (at most 1048576 entries of C)");
     return SKINNY_BAD_ARG;
   }
+  const size_t per_cta = (size_t)M * (size_t)N * sizeof(double);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
@@ -101,8 +108,8 @@ extern "C" skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K
   if (pl.grid > max_grid) pl.grid = (int)max_grid;  // fewer CTAs so the partials fit
 
   cudaStream_t st = (cudaStream_t)stream;
-  // ticket counters and the error word must start at zero; earlier calls leave them behind
-  if (cudaMemsetAsync(sd->base, 0, kStaticHeaderBytes, st) != cudaSuccess) {
+  // the ticket counters must start at zero; an earlier call that timed out leaves them behind
+  if (cudaMemsetAsync(sd->base, 0, kStaticCounterBytes, st) != cudaSuccess) {
     cudaGetLastError();
     set_error("static TSMTTSM: clearing the scratch header failed");
     return SKINNY_DEVICE_ERROR;
@@ -132,6 +139,39 @@ extern "C" skinny_status skinny_tsmttsm_d_static(int64_t M, int64_t N, int64_t K
   a.smem_avail = (uint32_t)(pl.smem - SMEM_HEADER);
   a.partials = sd->base + kStaticHeaderBytes;
   a.counter = reinterpret_cast<unsigned*>(sd->base);
-  a.err = reinterpret_cast<int*>(sd->base + 256);
+  a.err = reinterpret_cast<int*>(sd->base + kStaticErrOffset);
+  a.polls = kWaitPolls;
   return tsmttsm_dispatch<double, double>(pl.tm, pl.tn, a, dim3(pl.grid, pl.groups), pl.smem, st);
+}
+
+extern "C" skinny_status skinny_tsmttsm_d_static_check(void* stream) {
+  set_error("");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("static TSMTTSM check: no current CUDA device");
+    return SKINNY_DEVICE_ERROR;
+  }
+  StaticDevice* sd = nullptr;
+  skinny_status s = static_setup(dev, sd);
+  if (s != SKINNY_OK) return s;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  int flag = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyFromSymbol(&flag, g_tsmttsm_scratch, sizeof(int), kStaticErrOffset, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_error(std::string("static TSMTTSM check: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    return SKINNY_DEVICE_ERROR;
+  }
+  if (flag == 0) return SKINNY_OK;
+  const int zero = 0;
+  if (cudaMemcpyToSymbol(g_tsmttsm_scratch, &zero, sizeof(int), kStaticErrOffset, cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    set_error("static TSMTTSM check: clearing the error word failed");
+    return SKINNY_DEVICE_ERROR;
+  }
+  set_error("a bounded device-side wait of skinny_tsmttsm_d_static timed out");
+  return SKINNY_TIMEOUT;
 }

@@ -300,7 +300,7 @@ extern "C" skinny_status skinny_svqb(skinny_handle h, skinny_acc gram_acc, int64
                          M, st, o);
   if (s != SKINNY_OK) return s;
   const size_t smem = svqb_eig_smem((int)M);
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   ensure_smem_attr(svqb_eig_kernel, (int)smem, attr);
   svqb_eig_kernel<<<1, SVQB_THREADS, smem, st>>>(S, (int)M, T, info, 30);
   count_launch();
@@ -370,7 +370,7 @@ extern "C" skinny_status skinny_cholqr(skinny_handle h, skinny_acc gram_acc, int
   const double one = 1.0, zero = 0.0;
   LaunchOpts o{};
   const size_t smem = (size_t)2 * M * (M + 1) * sizeof(double);
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   ensure_smem_attr(cholqr_kernel, (int)smem, attr);
   for (int pass = 0; pass < passes; pass++) {
     skinny_status s = dispatch_product(h, false, SKINNY_R64, gram_acc, M, M, K, X, ldx, &one, X, ldx, &zero, S, M,

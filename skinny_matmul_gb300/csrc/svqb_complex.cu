@@ -249,7 +249,7 @@ extern "C" skinny_status skinny_svqb_z(skinny_handle h, skinny_acc gram_acc, int
     s = dispatch_conj(h, SKINNY_C64, SKINNY_ACC_NATIVE, M, M, K, X, ldx, one, X, ldx, zero, S, M, st);
   if (s != SKINNY_OK) return s;
   const size_t smem = eig_smem((int)M);
-  static std::atomic<int> attr{0};
+  static SmemAttr attr;
   ensure_smem_attr(svqbz_eig_kernel, (int)smem, attr);
   svqbz_eig_kernel<<<1, CTHREADS, smem, st>>>(S, (int)M, T, 30);
   count_launch();

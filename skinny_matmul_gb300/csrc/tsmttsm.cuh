@@ -40,6 +40,7 @@ struct TsmttsmArgs {
   void* partials;
   unsigned* counter;
   int* err;
+  uint32_t polls;  // poll limit of the bounded waits on the copy ring
 };
 
 template <typename T>
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(TSMTTSM_THREADS, 1) tsmttsm_kernel(const Tsmtt
 #pragma unroll
     for (int j = 0; j < TN; j++) acc[i][j] = O::zero();
 
-  bool bail = false;
+  int bail = -1;  // ring position whose wait gave up
   for (int i = 0; i < nt; i++) {
     const int64_t t = t_begin + i;
     const int s = i % p.stages;
@@ -155,9 +156,9 @@ __global__ void __launch_bounds__(TSMTTSM_THREADS, 1) tsmttsm_kernel(const Tsmtt
     T* As = stage_a(s);
     T* Bs = stage_b(s);
     if (is_bulk(t)) {
-      bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((i / p.stages) & 1), p.err);
+      bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((i / p.stages) & 1), p.err, p.polls);
       if (__syncthreads_or(!ok)) {
-        bail = true;
+        bail = i;
         break;
       }
     } else {
@@ -192,7 +193,15 @@ __global__ void __launch_bounds__(TSMTTSM_THREADS, 1) tsmttsm_kernel(const Tsmtt
       issue(t + p.stages, s);
     }
   }
-  if (bail) return;  // timeout recorded in *err; the host resets the ticket counter
+  if (bail >= 0) {
+    // Timeout recorded in *err; the host resets the ticket counter.  Copies already issued into
+    // the ring (positions bail .. bail + stages - 1) may still be landing in shared memory:
+    // wait for them, with the default bound, before the CTA exits.
+    if (tid == 0)
+      for (int j = bail; j < nt && j < bail + p.stages; j++)
+        if (is_bulk(t_begin + j)) mbar_wait_bounded(&bars[j % p.stages], (uint32_t)((j / p.stages) & 1), nullptr);
+    return;
+  }
 
   // ---- CTA reduction ------------------------------------------------------------------------
   // The phases reduce into shared memory when (MN + NT) entries fit in the ring, otherwise

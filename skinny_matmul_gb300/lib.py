@@ -82,6 +82,7 @@ SIGNATURES = {
     "skinny_status_string": (ctypes.c_char_p, [_i]),
     "skinny_last_error": (ctypes.c_char_p, []),
     "skinny_check_device": (_i, [_vp]),
+    "skinny_set_wait_limit": (_i, [_vp, ctypes.c_uint32]),
     "skinny_kernel_launches": (ctypes.c_uint64, []),
     "skinny_tsmttsm": (_i, _PROD),
     "skinny_tsmttsm_conj": (_i, _PROD),
@@ -103,6 +104,7 @@ SIGNATURES = {
     "skinny_group": (_i, [_vp, _i, ctypes.POINTER(GroupItem), ctypes.c_int32, _vp]),
     "skinny_tsmttsm_d_static": (_i, [_i64, _i64, _i64, _vp, _i64, ctypes.c_double, _vp, _i64,
                                      ctypes.c_double, _vp, _i64, _vp]),
+    "skinny_tsmttsm_d_static_check": (_i, [_vp]),
     "skinny_tsmttsm_s": (_i, _ref_sig(ctypes.c_float, ctypes.c_float)),
     "skinny_tsmttsm_d": (_i, _ref_sig(ctypes.c_double, ctypes.c_double)),
     "skinny_tsmttsm_c": (_i, _ref_sig(c32, c32)),
