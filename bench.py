@@ -9,8 +9,13 @@ in-place form (C = A) for every M = N; entries U[-1,1) from a seeded generator. 
 shape once.  Each shape's operands are larger than L2 (129 MB), so no L2 flush is needed.
 
 The default line also carries "split_vs_fp64" (TSMTTSM FP64 64x64, K = 2^24, s*2^e entries: plain
-FP64 vs split precision vs double-double, with errors) and "serving" (600 requests of the serving
+FP64 vs split precision vs double-double, with errors), "tsmttsm_sweep" (the metric's TSMTTSM half:
+FP64 M = N in {1..64} with A and B of 1 GiB, and C1) and "serving" (600 requests of the serving
 mix through the request loop vs one launch per call); --no-extras skips them.
+
+The reference arm (--impl reference) times the oracle port of the reference's loops on the host
+cores (its value) and, on the default workload, the reference's own GPU kernels on the same box
+("gpu_kernels": compiled from its headers into oracle/_ref, best variant and blockCount per shape).
 
 Other workloads: "tsmttsm-c1" (TSMTTSM FP64 8x8, K = 2^20, 16 rotating input copies),
 "precision-c3" (M = N in {32, 64, 128}), "svqb-c4", "serve-c5" (2000 requests), and probes for ncu.
@@ -154,6 +159,51 @@ def c5_items():
                  bytes=r["bytes"], flops=0) for r in reqs[:20]]
 
 
+TS_SWEEP = (1, 2, 4, 8, 16, 32, 64)
+
+
+def tsmttsm_sweep_items():
+    """TSMTTSM FP64 C(MxM) = A^T B, M = N in {1..64}, A and B of 1 GiB each, alpha 1, beta 0."""
+    items = []
+    for M in TS_SWEEP:
+        K = (1 << 30) // (8 * M)
+        items.append(dict(op="tsmttsm", dt="f64", M=M, N=M, K=K, inplace=False, s=8, bytes=2 * M * K * 8,
+                          flops=2 * M * M * K, copies=1))
+    return items
+
+
+def tsmttsm_sweep(h, dev, reps=5):
+    """The metric's TSMTTSM half: every shape of tsmttsm_sweep_items() plus C1 (8 x 8, K = 2^20, 16
+    rotating input copies so the inputs exceed L2), each with the library's choice (auto) and the
+    CUDA-core FP64 kernel (native); median of `reps` CUDA-event timings after two warm-ups."""
+    import torch
+    hbm, _ = peaks()
+    rows = []
+    for it in tsmttsm_sweep_items() + c1_items():
+        ops = make_operands(it, dev, 500 + it["M"])
+        row = {"M": it["M"], "N": it["N"], "K": it["K"], "config": "C1" if it.get("copies", 1) > 1 else "1 GiB"}
+        for method in ("auto", "native"):
+            for i in range(2):
+                call(h, it, ops, i, method)
+            ts = []
+            for i in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                call(h, it, ops, i, method)
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) * 1e-3)
+            t = sorted(ts)[len(ts) // 2]
+            gbs = it["bytes"] / t / 1e9
+            row[method] = {"us": round(t * 1e6, 1), "GB/s": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4),
+                           "fp64_equivalent_tflops": round(it["flops"] / t / 1e12, 3),
+                           "kernel": kernel_of(it, method)}
+        rows.append(row)
+        del ops
+        torch.cuda.empty_cache()
+    return rows
+
+
 def probe_tsmm_items():
     M = N = 8
     K = 1 << 22
@@ -201,6 +251,8 @@ WORKLOADS = {
     "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),
     "tsmm-sweep": (sweep_items, "TSMM FP64 + complex FP64, alpha 1, beta 0.5, A = 1 GiB per shape, "
                    "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
+    "tsmttsm-sweep": (tsmttsm_sweep_items, "TSMTTSM FP64 C(MxM) = A^T B, M = N in {1..64}, A and B of 1 GiB "
+                      "each, alpha 1, beta 0"),
     "tsmttsm-c1": (c1_items, "TSMTTSM FP64 C(8x8) = A^T B, K = 2^20, alpha 1, beta 0, "
                    "16 rotating input copies (2 GiB > L2)"),
     "group-small": (c5_items, "the serving mix's small requests (TSMTTSM / TSMM of cost <= 32 MiB, FP64 / complex "
@@ -359,9 +411,98 @@ def sum_over_ranks(v, world):
     return float(t.item())
 
 
+REF_TSMM_VARIANTS = {False: ("FIX3", "FIX_FB"), True: ("FIX3", "FIX_IP_GHOST")}
+REF_TSMTTSM_VARIANTS = ("GENV5", "GENV3X", "SPECSMALL")
+
+
+def reference_gpu_kernels(items, reps=3):
+    """The reference's own GPU kernels (its headers compiled for sm_103a into oracle/_ref) timed on
+    this machine's GPU, on the workload's real FP64 shapes they cover (the reference has no complex
+    out-of-place TSMM kernel among those built, and GENV5 / SPECSMALL stop at M, N = 32), with its
+    perf harness's launch search (perf.cu:166-190): blockCount = 1..8 x SMs, median of 3, best.
+    Operands get the padding those kernels' over-reads need; alpha 1, beta 0.5 (TSMM) / 0 (TSMTTSM)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        from oracle import ref_gpu
+        msg = ref_gpu.init()
+        if msg:
+            return {"unavailable": msg}
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    hbm, _ = peaks()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    out, tot_b, tot_t = [], 0.0, 0.0
+    g = torch.Generator(device="cuda").manual_seed(99)
+    for it in items:
+        if it["dt"] != "f64":
+            continue
+        M, N, K = it["M"], it["N"], it["K"]
+        tsmm = it["op"] == "tsmm"
+        if not tsmm and max(M, N) > 32:
+            continue
+        copies = it.get("copies", 1)
+
+        def rnd(n):
+            t = ref_gpu.padded(n, torch.float64)
+            t.copy_(torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
+            return t
+        if tsmm:
+            A = [rnd(K * M)]
+            B = [rnd(M * N)]
+            C = A[0] if it["inplace"] else rnd(K * N)
+            variants = REF_TSMM_VARIANTS[it["inplace"]]
+        else:
+            A = [rnd(K * M) for _ in range(copies)]
+            B = [rnd(K * N) for _ in range(copies)]
+            C = rnd(M * N)
+            variants = REF_TSMTTSM_VARIANTS
+        temp = torch.empty(8 * sms * N * M * 8 + 256, dtype=torch.uint8, device="cuda")
+        best = {}
+        for v in variants:
+            for bc in ([sms] if v == "FIX_IP_GHOST" else [sms * m for m in range(1, 9)]):
+                ts = []
+                for r in range(reps + 1):
+                    j = r % copies
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    if tsmm:
+                        ok = ref_gpu.tsmm(v, M, N, K, A[0], M, 1.0, B[0], M, 0.5, C, M if it["inplace"] else N, bc)
+                    else:
+                        ok = ref_gpu.tsmttsm(v, M, N, K, A[j], M, 1.0, B[j], N, 0.0, C, M, bc, temp=temp)
+                    e1.record()
+                    e1.synchronize()
+                    if not ok:
+                        break
+                    if r:
+                        ts.append(e0.elapsed_time(e1) * 1e-3)
+                if not ts:
+                    continue
+                t = sorted(ts)[len(ts) // 2]
+                if v not in best or t < best[v][0]:
+                    best[v] = (t, bc)
+        del A, B, C, temp
+        torch.cuda.empty_cache()
+        if not best:
+            continue
+        vbest = min(best, key=lambda k: best[k][0])
+        t, bc = best[vbest]
+        gbs = it["bytes"] / t / 1e9
+        tot_b += it["bytes"]
+        tot_t += t
+        out.append({"op": it["op"], "M": M, "N": N, "K": K, "inplace": it["inplace"], "best": vbest,
+                    "blockCount": bc, "us": round(t * 1e6, 1), "GB/s": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4),
+                    "variants_GBs": {k: round(it["bytes"] / v[0] / 1e9, 1) for k, v in best.items()}})
+    return {"what": "the reference's own GPU kernels, compiled from its headers for sm_103a, best variant and "
+                    "blockCount per shape (its perf harness's search)",
+            "aggregate_GBs": round(tot_b / tot_t / 1e9, 1) if tot_t else None, "shapes": out}
+
+
 def run_reference(args):
     """The reference arm: the reference has no CPU implementation of its products (its own oracle
-    is cuBLAS), so this arm times the oracle port of its loops on the host cores."""
+    is cuBLAS), so this arm times the oracle port of its loops on the host cores.  Beside that
+    value it reports the reference's own GPU kernels on the same box (reference_gpu_kernels)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -382,6 +523,8 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.workload == "tsmm-sweep" and not args.no_extras:
+        line["gpu_kernels"] = reference_gpu_kernels(items + tsmttsm_sweep_items() + c1_items())
     print(json.dumps(line), flush=True)
 
 
@@ -520,6 +663,10 @@ def main():
             "native_ms": byk["native"]["ms"], "split_ms": byk["split"]["ms"], "dd_ms": byk["dd"]["ms"],
             "speedup": byk["split"]["speedup_vs_native"], "split_err": byk["split"]["normwise_err_vs_dd"],
             "native_err": byk["native"]["normwise_err_vs_dd"]}
+        extras["tsmttsm_sweep"] = {
+            "config": "TSMTTSM FP64 C(MxM) = A^T B, M = N in {1..64}, A and B of 1 GiB each (> L2), plus C1 "
+                      "(8 x 8, K = 2^20, 16 rotating copies); auto = the library's choice, native = CUDA-core FP64",
+            "shapes": tsmttsm_sweep(h, dev)}
         seq, srv, _, wall_srv = serve_measure(h, dev, 600, 2000.0, rank)
         extras["serving"] = {
             "config": "600 requests of the serving mix (Poisson, 2000/s), operands resident in HBM",

@@ -30,6 +30,32 @@ struct __align__(2 * sizeof(R)) cplxh {
 typedef cplxh<float> c32h;
 typedef cplxh<double> c64h;
 
+// One entry of alpha*B + beta*I (in-place TSMM with M == N: C = A (alpha B + beta I)): alpha*b,
+// plus beta on the diagonal (one rounding for real types)
+__device__ __forceinline__ float fold_entry(float a, float b, float be, bool diag) {
+  return diag ? fmaf(a, b, be) : a * b;
+}
+__device__ __forceinline__ double fold_entry(double a, double b, double be, bool diag) {
+  return diag ? fma(a, b, be) : a * b;
+}
+template <typename C>
+__device__ __forceinline__ C fold_entry_c(C a, C b, C be, bool diag) {
+  C r = {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+  if (diag) {
+    r.x += be.x;
+    r.y += be.y;
+  }
+  return r;
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> fold_entry(cplx<R> a, cplx<R> b, cplx<R> be, bool diag) {
+  return fold_entry_c(a, b, be, diag);
+}
+template <typename R>
+__device__ __forceinline__ cplxh<R> fold_entry(cplxh<R> a, cplxh<R> b, cplxh<R> be, bool diag) {
+  return fold_entry_c(a, b, be, diag);
+}
+
 // ---------------------------------------------------------------- double-double primitives
 __device__ __forceinline__ dd dd_fast2sum(double a, double b) {
   double s = __dadd_rn(a, b);

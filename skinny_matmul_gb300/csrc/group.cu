@@ -236,9 +236,12 @@ __device__ void tsmm_unit(const GroupDesc& g, int64_t ul, unsigned char* smem) {
   T* Bs = reinterpret_cast<T*>(smem);
   const T* B = static_cast<const T*>(g.B);
   const int64_t ldb = g.ldb;
+  const T alpha = scal<T>(g.alpha), beta = scal<T>(g.beta);
+  const bool fold = (code & GF_FOLD) != 0;  // the same fold as tsmm_kernel, so the bits agree
   for (int e = tid; e < M * np; e += GT) {
     const int m = e / np, n = e - m * np;
-    Bs[e] = (n < N) ? B[(int64_t)n * ldb + m] : tzero<T>();
+    const T b = (n < N) ? B[(int64_t)n * ldb + m] : tzero<T>();
+    Bs[e] = (fold && n < N) ? fold_entry(alpha, b, beta, m == n) : b;
   }
   __syncthreads();
   const T* A = static_cast<const T*>(g.A);
@@ -247,8 +250,7 @@ __device__ void tsmm_unit(const GroupDesc& g, int64_t ul, unsigned char* smem) {
   const int RS = GT / gn;
   const int cell = tid % gn, rs = tid / gn;
   const int n0 = cell * TN;
-  const T alpha = scal<T>(g.alpha), beta = scal<T>(g.beta);
-  const bool bz = (code & GF_BZERO) != 0, alpha_one = O::is_one(alpha);
+  const bool bz = fold || (code & GF_BZERO) != 0, alpha_one = fold || O::is_one(alpha);
   const int64_t rb = ul * g.rows, re = min(g.K, rb + g.rows);
   for (int64_t base = rb; base < re; base += RS) {  // the same trip count for every lane
     const int64_t r = base + rs;
@@ -487,6 +489,7 @@ skinny_status group_plan(const skinny_group_item* items, const skinny_dtype* dts
         rows = round_up(std::max<int64_t>(RS, UNIT_BYTES / rc), RS);
         units = (it.K + rows - 1) / rows;
         code |= GF_TSMM | (ilog2(tn) << 4) | (gn << 8);
+        if (it.A == it.C && it.lda == it.ldc && it.M == it.N && !bz) code |= GF_FOLD;
       } else {
         const bool gram = it.A == it.B && it.lda == it.ldb && it.M == it.N;
         const int tt = std::min(pow2ceil(std::min(it.M, it.N)), cap_t);

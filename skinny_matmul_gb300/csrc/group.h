@@ -22,7 +22,8 @@ constexpr int GROUP_SMEM = 2 * GROUP_TILE;   // dynamic shared memory per CTA
 constexpr int GROUP_MAX_W = 64;              // M, N limit of a grouped problem
 constexpr int GROUP_CLASSES = 4;             // R32, R64, C32, C64
 
-enum : int32_t { GF_TSMM = 1, GF_GRAM = 2, GF_BZERO = 4 };
+// GF_FOLD: in-place TSMM with M == N and beta != 0, computed as C = A (alpha B + beta I)
+enum : int32_t { GF_TSMM = 1, GF_GRAM = 2, GF_BZERO = 4, GF_FOLD = 8 };
 
 struct GroupHeader {
   int32_t first[GROUP_CLASSES];  // first descriptor of each class

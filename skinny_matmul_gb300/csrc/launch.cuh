@@ -13,6 +13,7 @@
 #include "skinny.h"
 #include "tsmm.cuh"
 #include "tsmttsm.cuh"
+#include "tsmttsm_rows.cuh"
 
 namespace skinny {
 
@@ -183,12 +184,101 @@ skinny_status tsmttsm_plan(const DeviceInfo& dev, int64_t M, int64_t N, int64_t 
   return SKINNY_OK;
 }
 
+// ----------------------------------------------------------------- TSMTTSM, narrow products
+// Register-tile entries a thread of the row-streaming kernel may hold: 64 for 4- and 8-byte
+// accumulators (FP64 8 x 8), 16 for 16-byte ones (complex FP64, double-double).
+template <typename Acc>
+constexpr int rows_cap() {
+  return sizeof(Acc) <= 8 ? 64 : 16;
+}
+
+// The row-streaming kernel takes a product when both padded widths are <= 8 and their tile fits
+// rows_cap; an autotuned row-tile size asks for the ring kernel instead.
+template <typename T, typename Acc>
+bool rows_eligible(int64_t M, int64_t N, bool gram, const LaunchOpts& o) {
+  if (o.rows_per_tile > 0 || M < 1 || N < 1 || M > 8 || N > 8) return false;
+  int tm = pow2ceil(M), tn = pow2ceil(N);
+  if (gram) tm = tn = std::max(tm, tn);
+  return tm * tn <= rows_cap<Acc>();
+}
+
+template <typename T, typename Acc, int TM, int TN>
+skinny_status tsmttsm_rows_launch(RowsArgs<T>& a, const DeviceInfo& dev, Workspace& ws, int bps_opt,
+                                  cudaStream_t st) {
+  if constexpr (TM * TN > rows_cap<Acc>()) {
+    set_error("tsmttsm: register tile too large for the accumulator type");
+    return SKINNY_UNSUPPORTED;
+  } else {
+    constexpr int U = TM * TN <= 2 ? 4 : (TM * TN <= 8 ? 2 : 1);
+    auto kern = tsmttsm_rows_kernel<T, Acc, TM, TN, U>;
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ROWS_THREADS, 0);
+    if (occ < 1) occ = 1;
+    if (bps_opt > 0 && bps_opt < occ) occ = bps_opt;
+    const int64_t per_cta = (int64_t)ROWS_THREADS * U;
+    int64_t grid = std::min<int64_t>((int64_t)dev.sms * occ, (a.K + per_cta - 1) / per_cta);
+    if (grid < 1) grid = 1;
+    skinny_status s = workspace_ensure(ws, (size_t)grid * (size_t)(a.M * a.N) * sizeof(Acc), st);
+    if (s != SKINNY_OK) return s;
+    a.partials = ws.partials;
+    a.counter = ws.counter;
+    kern<<<(int)grid, ROWS_THREADS, 0, st>>>(a);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(std::string("tsmttsm launch: ") + cudaGetErrorString(e));
+      return SKINNY_DEVICE_ERROR;
+    }
+    return SKINNY_OK;
+  }
+}
+
+template <typename T, typename Acc>
+skinny_status tsmttsm_rows_run(const DeviceInfo& dev, Workspace& ws, cudaStream_t st, int64_t M, int64_t N,
+                               int64_t K, const T* A, int64_t lda, T alpha, const T* B, int64_t ldb, T beta,
+                               bool beta_zero, T* C, int64_t ldc, bool gram, const LaunchOpts& o) {
+  int tm = pow2ceil(M), tn = pow2ceil(N);
+  if (gram) tm = tn = std::max(tm, tn);
+  RowsArgs<T> a;
+  a.A = A;
+  a.B = B;
+  a.C = C;
+  a.K = K;
+  a.lda = lda;
+  a.ldb = ldb;
+  a.ldc = ldc;
+  a.M = (int)M;
+  a.N = (int)N;
+  a.alpha = alpha;
+  a.beta = beta;
+  a.beta_zero = beta_zero;
+  a.gram = gram;
+  // 16-byte pairs: FP64, an aligned base, an even leading dimension covering the padded width
+  const bool f64 = std::is_same<T, double>::value;
+  a.vec_a = f64 && tm >= 2 && (uintptr_t)A % 16 == 0 && lda % 2 == 0 && lda >= tm;
+  a.vec_b = f64 && tn >= 2 && (uintptr_t)B % 16 == 0 && ldb % 2 == 0 && ldb >= tn;
+  a.partials = nullptr;
+  a.counter = nullptr;
+  const int b = o.blocks_per_sm;
+#define SK_ROWS(X, Y) \
+  if (tm == X && tn == Y) return tsmttsm_rows_launch<T, Acc, X, Y>(a, dev, ws, b, st);
+  SK_ROWS(1, 1) SK_ROWS(1, 2) SK_ROWS(1, 4) SK_ROWS(1, 8)
+  SK_ROWS(2, 1) SK_ROWS(2, 2) SK_ROWS(2, 4) SK_ROWS(2, 8)
+  SK_ROWS(4, 1) SK_ROWS(4, 2) SK_ROWS(4, 4) SK_ROWS(4, 8)
+  SK_ROWS(8, 1) SK_ROWS(8, 2) SK_ROWS(8, 4) SK_ROWS(8, 8)
+#undef SK_ROWS
+  set_error("tsmttsm: no compiled row tile");
+  return SKINNY_UNSUPPORTED;
+}
+
 template <typename T, typename Acc>
 skinny_status tsmttsm_run(const DeviceInfo& dev, Workspace& ws, int* err, cudaStream_t st,
                           int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, T alpha,
                           const T* B, int64_t ldb, T beta, bool beta_zero, T* C, int64_t ldc,
                           const LaunchOpts& o) {
   const bool gram = (A == B) && (lda == ldb) && (M == N);
+  if (rows_eligible<T, Acc>(M, N, gram, o))
+    return tsmttsm_rows_run<T, Acc>(dev, ws, st, M, N, K, A, lda, alpha, B, ldb, beta, beta_zero, C, ldc, gram, o);
   TsmttsmPlan pl;
   skinny_status s = tsmttsm_plan<T, Acc>(dev, M, N, K, A, lda, B, ldb, gram, o, pl);
   if (s != SKINNY_OK) return s;
@@ -280,6 +370,8 @@ skinny_status tsmm_run(const DeviceInfo& dev, cudaStream_t st, int64_t M, int64_
   a.alpha = alpha;
   a.beta = beta;
   a.beta_zero = beta_zero;
+  // in place with M == N: C = A (alpha B + beta I), folded while B is staged
+  a.fold = (const void*)A == (const void*)C && lda == ldc && M == N && !beta_zero && sizeof(Acc) == sizeof(T);
   a.gn = gn;
   a.np = np;
   const int sm = (int)(smem < 16 ? 16 : smem);

@@ -30,7 +30,9 @@
 //     chunk before the TMEM loads of the chunk before it (16-byte pieces where rows are aligned),
 //     so that global and TMEM latencies overlap.
 //   * |D_L| <= 2^22 for contraction widths <= 32 (converted with a float add), <= 2^23 for 64
-//     (converted with cvt.rni); both exact.
+//     (converted with integer instructions from the FP32 bit pattern); both exact.
+//   * In place with M == N, beta is folded into the diagonal of alpha*B before slicing
+//     (C = A (alpha B + beta I)), so the epilogue neither reads C nor runs the beta FMA.
 // Complex FP64 (interleaved) runs as the real product of doubled width: A (K x 2M), B' (2M x 2N)
 // with B'[2n][2m] = br, B'[2n][2m+1] = -bi, B'[2n+1][2m] = bi, B'[2n+1][2m+1] = br, C (K x 2N).
 // Inputs must be finite.
@@ -62,6 +64,7 @@ struct Args {
   int cplx;                  // B is complex (alpha, beta complex)
   double alpha[2], beta[2];
   int beta_zero, inplace, vec;  // vec: rows of A may be read as 16-byte pairs
+  int fold;                     // beta folded into B's diagonal (in place, M == N); beta_zero then set
   int vecc;                     // rows of C may be read and written as 16-byte pairs
   int64_t ntiles;
   uint32_t abuf;  // bytes of one A' buffer
@@ -127,13 +130,21 @@ __device__ __forceinline__ uint32_t kmaj(int row, int koct, uint32_t lbo) {
   return (uint32_t)koct * lbo + (uint32_t)(row >> 3) * 128u + (uint32_t)(row & 7) * 16u;
 }
 
-// value of (alpha * B) at (m, n) in the real view, 0 outside M x N
+// value of (alpha * B + fold * I) at (m, n) in the real view, 0 outside M x N; fold is beta for
+// the in-place product with M == N (C = A (alpha B + beta I)), else 0
 __device__ __forceinline__ double alpha_b(const Args& p, int m, int n) {
   if (m >= p.M || n >= p.N) return 0.0;
-  if (!p.cplx) return p.B[(int64_t)n * p.ldb + m] * p.alpha[0];
+  if (!p.cplx) {
+    const double v = p.B[(int64_t)n * p.ldb + m] * p.alpha[0];
+    return (p.fold && m == n) ? v + p.beta[0] : v;
+  }
   const int nc = n >> 1, mc = m >> 1;
   const double br = p.B[2 * ((int64_t)nc * p.ldb + mc)], bi = p.B[2 * ((int64_t)nc * p.ldb + mc) + 1];
-  const double ar = br * p.alpha[0] - bi * p.alpha[1], ai = br * p.alpha[1] + bi * p.alpha[0];
+  double ar = br * p.alpha[0] - bi * p.alpha[1], ai = br * p.alpha[1] + bi * p.alpha[0];
+  if (p.fold && mc == nc) {
+    ar += p.beta[0];
+    ai += p.beta[1];
+  }
   return ((n & 1) == 0) ? ((m & 1) == 0 ? ar : -ai) : ((m & 1) == 0 ? ai : ar);
 }
 
@@ -173,6 +184,17 @@ __device__ __forceinline__ double i64_to_double(long long x, int E) {
   return x ? r : 0.0;
 }
 
+// The integer value of an FP32 holding an exact integer with |f| < 2^24, with integer instructions
+// only (a float-to-int conversion instruction shares GB300's narrow FP64 pipe, the unit the beta
+// FMA already needs): the mantissa with its implicit bit, shifted right by 150 - exponent (a
+// funnel shift that clamps at 32, so 0.0 gives 0), then the sign.
+__device__ __forceinline__ int f32_int_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t mag = __funnelshift_rc((u & 0x7FFFFFu) | 0x800000u, 0u, 150u - ((u >> 23) & 0xFFu));
+  const int s = (int)u >> 31;  // 0 or -1
+  return ((int)mag ^ s) - s;
+}
+
 // The double of column x of a chunk: V = sum_L D_L 2^(8(9-L)) from the eight FP32 level sums in
 // raw[L][x] (exact integers), times 2^E.
 template <int MP>
@@ -182,7 +204,7 @@ __device__ __forceinline__ double level_value(const uint32_t (&raw)[8][8], int x
   for (int L = 0; L < 8; L++) {
     const float f = __uint_as_float(raw[L][x]);
     // |D_L| <= (L-1) * MP * 2^14: up to 2^22 the magic add is exact (levels 2..5 at MP = 64)
-    dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : __float2int_rn(f);
+    dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : f32_int_exact(f);
   }
   // level pairs in 32 bits: |D_L * 256 + D_{L+1}| < 2^31 for every pair (the largest, D_8 * 256 +
   // D_9 at MP = 64, is below 1.9e9)
@@ -542,6 +564,9 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   std::memcpy(a.beta, beta, cplx ? 16 : 8);
   a.beta_zero = a.beta[0] == 0.0 && a.beta[1] == 0.0;
   a.inplace = (const void*)A == (const void*)C;
+  // in place with M == N: C = A (alpha B + beta I); the epilogue then needs no old C and no FMA
+  a.fold = a.inplace && M == N && !a.beta_zero;
+  if (a.fold) a.beta_zero = 1;
   a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
   a.vecc = ((uintptr_t)C % 16 == 0) && (a.ldc % 2 == 0);
   a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x fp16

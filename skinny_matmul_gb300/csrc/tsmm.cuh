@@ -14,6 +14,9 @@
 //     passes __syncwarp(), and only then are outputs written; rows never cross warps, so no
 //     output can overwrite input that another thread still needs.  beta*C reads the element the
 //     same thread then overwrites.
+//   * In place with M == N (and accumulation in the working type), beta is folded into B's diagonal
+//     while B is staged: C = A (alpha B + beta I), so the epilogue neither reads C nor runs the
+//     beta FMA on the FP64 pipe.
 //   * Rows are distributed grid-stride over a persistent grid, U rows per thread and step (U = 4
 //     for narrow widths so that enough loads are in flight to stream at HBM speed); all lanes of
 //     a warp run the same trip count so the __syncwarp() is always reached by the full warp.
@@ -32,6 +35,7 @@ struct TsmmArgs {
   int M, N;
   T alpha, beta;
   int beta_zero;
+  int fold;  // Bs = alpha B + beta I (in place, M == N); the epilogue then writes the sums as they are
   int gn;  // cells per row (power of two, <= 32)
   int np;  // padded width of Bs (gn * TN)
 };
@@ -45,9 +49,15 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
   extern __shared__ __align__(128) unsigned char smem[];
   T* Bs = reinterpret_cast<T*>(smem);
   const int M = p.M, N = p.N, np = p.np, gn = p.gn;
+  const bool fold = p.fold != 0;
   for (int e = threadIdx.x; e < M * np; e += NT) {
     int m = e / np, n = e - m * np;
-    Bs[e] = (n < N) ? p.B[(int64_t)n * p.ldb + m] : tzero<T>();
+    const T b = (n < N) ? p.B[(int64_t)n * p.ldb + m] : tzero<T>();
+    if constexpr (sizeof(Acc) == sizeof(T)) {
+      Bs[e] = (fold && n < N) ? fold_entry(p.alpha, b, p.beta, m == n) : b;
+    } else {
+      Bs[e] = b;
+    }
   }
   __syncthreads();
 
@@ -57,7 +67,7 @@ __global__ void __launch_bounds__(TSMM_THREADS) tsmm_kernel(const TsmmArgs<T> p)
   const int cell = threadIdx.x % gn, rs = threadIdx.x / gn;
   const int n0 = cell * TN;
   const int64_t step = (int64_t)gridDim.x * RS * U;
-  const bool alpha_one = O::is_one(p.alpha), bz = p.beta_zero != 0;  // decided once
+  const bool alpha_one = fold || O::is_one(p.alpha), bz = fold || p.beta_zero != 0;  // decided once
   for (int64_t base = (int64_t)blockIdx.x * RS * U; base < p.K; base += step) {
     bool valid[U];
 #pragma unroll

@@ -1,6 +1,7 @@
 """Failure detection without a GPU fault: a bounded device-side wait that runs out.
 
-The CUDA-core TSMTTSM kernel waits on mbarriers for the bulk copies of its row ring.  With the
+The CUDA-core TSMTTSM ring kernel (products wider than 8, or above the row-streaming kernel's
+register tile) waits on mbarriers for the bulk copies of its row ring.  With the
 handle's poll limit set to 0 every such wait gives up at once; the kernel records SKINNY_TIMEOUT
 in the handle's device error word, waits (with the default bound) for the copies it has already
 issued, and exits without writing C.  The host reads the status with skinny_check_device, which
@@ -22,7 +23,7 @@ def test_wait_timeout_is_reported_and_the_next_call_is_correct():
     h = Handle(0)
     try:
         rng = np.random.default_rng(11)
-        M = N = 8
+        M = N = 16  # the ring kernel (narrower products stream rows without waits)
         K = 1 << 18  # many full row tiles per CTA: the ring is fed by bulk copies
         A = rng.uniform(-1, 1, K * M)
         B = rng.uniform(-1, 1, K * N)
@@ -52,7 +53,7 @@ def test_gram_and_float_paths_recover_after_timeouts():
     h = Handle(0)
     try:
         rng = np.random.default_rng(12)
-        for dt, M in ((np.float64, 16), (np.float32, 8)):
+        for dt, M in ((np.float64, 16), (np.float32, 16)):
             K = 300007
             X = rng.uniform(-1, 1, K * M).astype(dt)
             Xd = torch.from_numpy(X).cuda()
