@@ -2,29 +2,39 @@
 // counterpart in the reference, whose FP64 kernels are CUDA-core DFMA loops, e.g.
 // tsmttsm/genv5.cuh:28-89).  Wider products go to split_wide.cu.
 //
-// Why: GB300 executes 595 G FP64 FMA/s but 2.25 P FP16 / BF16 tensor flop/s.  A CUDA-core FP64 TSMTTSM
-// is FP64-bound for every M = N >= 2.  Here each FP64 product is computed exactly from 8-bit
-// pieces on the tensor cores, and FP64 arithmetic is used only a few times per 1024 rows.
+// Why: GB300 executes 595 G FP64 FMA/s but 2.25 P FP16 / BF16 tensor flop/s.  A CUDA-core FP64
+// TSMTTSM is FP64-bound for every M = N >= 2.  Here each FP64 product is computed exactly from
+// 8-bit pieces on the tensor cores, and FP64 arithmetic is used only a few times per 1024 rows.
 //
 // Scheme (Ozaki-style error-free splitting, written for this kernel):
-//   * Per column m of A (and n of B) a shared exponent E is kept: the largest exponent field
-//     seen in the current accumulation period.  Each element x is written as a 62-bit fixed-point
-//     integer F = |x| * 2^(1084 - E) (< 2^62) and F as 8 balanced base-256 digits
-//     d_1..d_8 in [-128, 128] (d_1 most significant): x = sign * sum_i d_i 2^(8(8-i)) 2^(E-1084).
-//     Digits are exact in FP16 (formed with byte permutes, digits.cuh).
+//   * Per column m of A (and n of B) a shared exponent E holds for an epoch: each element x is a
+//     62-bit fixed-point integer F = |x| * 2^(1084 - E) written as 8 balanced base-256 digits
+//     d_1..d_8 (d_1 most significant): x = sign * sum_i d_i 2^(8(8-i)) 2^(E-1084).  Digits are
+//     exact in FP16 (byte permutes, digits.cuh).  When a round of rows holds an element above
+//     2^E's range, that column's E is raised with HEAD bits of headroom and a new period starts.
 //   * Digit planes are stacked along the MMA dimensions: A rows (i-1)*MP + m, B rows
 //     (j-1)*NP + n, so one tcgen05.mma (M = 128, N = 8*NP, K = 16, FP16 x FP16 -> FP32 in TMEM)
 //     forms every digit-pair product d_i(a) d_j(b) for 16 rows of K.
 //   * |d_i d_j| <= 2^14, so over a period of <= 1024 rows every partial sum is an integer of
-//     magnitude <= 2^24: the FP32 accumulation in TMEM is exact.  A period ends after 1024 rows,
-//     or earlier when a window raises a column's exponent.
-//   * Drain: TMEM -> registers -> int32; level sums S_L = sum_{i+j=L} D_ij (L = 2..9) are formed
-//     with a per-lane rotation and warp shuffles, then in shared memory with integer atomics;
-//     V = sum_L S_L 2^(8(16-L)) is assembled from two int64 words and added to an FP64 accumulator
-//     per C entry with weight 2^(EA+EB-2168).  Levels L >= 10 are dropped: their weight is below
-//     2^-56 of the leading level.
-//   * K rows stream in windows of 128 rows through a ring of FP64 tiles (1-D TMA bulk copies);
-//     digit buffers are double-buffered so slicing window w+1 overlaps the MMAs of window w.
+//     magnitude <= 2^24: the FP32 accumulation in TMEM is exact.  Two accumulator sets alternate
+//     between periods, so the drain of one period runs while the MMAs of the next proceed.
+//   * Drain: TMEM -> int32; level sums S_L = sum_{i+j=L} D_ij (L = 2..9) are formed with a
+//     per-lane rotation and warp shuffles, then in shared memory with integer atomics;
+//     V = sum_L S_L 2^(8(16-L)) is assembled from two int64 words and added to an FP64
+//     accumulator per C entry with weight 2^(EA+EB-2168).  Levels L >= 10 are dropped: their
+//     weight is below 2^-56 of the leading level (2^-52 with the headroom).
+//   * Warp roles, hand-offs through mbarriers (no CTA-wide barrier while streaming):
+//       warps 0-7  slicers: per round of rr rows (rr * (M + N) / 8 units of one column and 8 rows,
+//                  at most two per thread) read the FP64 values from the stage ring (or from
+//                  global memory where rows are not 16-byte aligned), check them against the
+//                  column exponents (one named barrier per round; two more only when a period
+//                  starts), slice them into a digit stage;
+//       warps 8-11 drain: one TMEM lane quadrant each;
+//       warp 12    producer: whole rounds of rows by 1-D TMA bulk copies into the FP64 ring;
+//       warp 13    MMA issuer: rr/16 MMAs per round into the period's accumulator set.
+//     The roles that wait most of the time (drain, producer, MMA) sleep between polls, so that
+//     their polling leaves issue slots to the slicers.  Every wait is bounded; a wait that runs
+//     out sets the error word, every role stops at its next wait, and the CTA writes no C.
 //   * Cross-CTA finish as in the CUDA-core kernel: CTA partials in FP64, the last CTA (ticket)
 //     sums them in CTA order, applies alpha/beta.
 // Inputs must be finite (Inf/NaN have no fixed-point form).
@@ -38,31 +48,42 @@ namespace skinny {
 
 namespace split {
 
-constexpr int W = 128;          // rows per window (8 MMA K-steps of 16)
-constexpr int PERIOD = 1024;    // rows accumulated exactly in TMEM
-constexpr int THREADS = 256;
+constexpr int PERIOD = 1024;   // rows accumulated exactly in TMEM (|sum| <= 1024 * 2^14)
 constexpr int DIGITS = 8;
-constexpr int OCT = W / 8;      // k-octets per window
-constexpr int DPAD = 128 * 16;  // slack after an A digit buffer: the MMA reads 128 rows per k-octet
-constexpr int HDR = 1024;       // barriers, TMEM slot, exponents
+constexpr int NSLICE = 8;      // slicer warps 0-7
+constexpr int NDRAIN = 4;      // drain warps 8-11 (one TMEM lane quadrant each)
+constexpr int WPROD = NSLICE + NDRAIN, WMMA = WPROD + 1;
+constexpr int THREADS = (WMMA + 1) * 32;  // 448
+constexpr int SLICERS = NSLICE * 32;
+constexpr int HEAD = 2;        // exponent headroom granted when a column's exponent is raised
+constexpr int MAXST = 4;       // FP64 stages (at most)
+constexpr int MAXDST = 3;      // digit stages (at most)
+constexpr int DPAD = 128 * 16; // slack after an A digit buffer: the MMA reads 128 rows per k-octet
+constexpr int HDR = 2048;      // barriers, TMEM slot, round and period records, exponents
 constexpr int SBYTES = 8 * 16 * 16 * 4;  // level sums S[8][16][16]
+constexpr int CBYTES = 256 * 8;          // FP64 accumulators of the C entries
+constexpr int STATIC_RESERVE = 1024;     // the kernel's static shared memory
+constexpr uint32_t SLEEP_DRAIN = 256;    // ns between polls of the drain warps (a period is ~8 rounds)
+constexpr uint32_t SLEEP_PRODUCER = 64;  // ns between polls of the producer warp
+constexpr uint32_t SLEEP_MMA = 32;       // ns between polls of the MMA thread
 
 struct Args {
   const double* A;
   const double* B;
   double* C;
   int64_t K, lda, ldb, ldc;
-  int M, N, MP;
+  int M, N, MP, NP;  // padded widths (powers of two); NP = MP in Gram mode
   double alpha, beta;
-  int beta_zero, gram, bulk, stages;
-  int64_t ntiles;
-  uint32_t tile_a, tile_b;  // bytes per FP64 stage (A, B), multiples of 128
-  int64_t lda_s, ldb_s;     // row strides of the FP64 stage tiles
-  int nmma;                 // MMA N (multiple of 16, >= 16)
-  int tmem_cols;
-  int sw;                   // windows per super-window (rows per iteration = sw * W)
-  uint32_t lbo_a, lbo_b;    // bytes between k-octets of the A / B digit buffers
-  uint32_t dig_a, dig_b;    // bytes of one A / B digit buffer (A includes DPAD)
+  int beta_zero, gram, bulk;
+  int stages, dstages;   // FP64 stages, digit stages
+  int rr;                // rows per round (a multiple of 128, <= PERIOD)
+  int64_t nrounds;
+  uint32_t stage_bytes;  // FP64 stage: rr rows of A (tile_a bytes), then rr rows of B
+  uint32_t tile_a;
+  int nmma;              // MMA N (multiple of 16, >= 16)
+  int tmem_cols;         // two accumulator sets of nmma columns
+  uint32_t lbo_a, lbo_b; // bytes between k-octets of the A / B digit buffers
+  uint32_t dig_a, dig_b; // bytes of one A / B digit buffer (A includes DPAD)
   double* partials;
   unsigned* counter;
   int* err;
@@ -149,44 +170,79 @@ __device__ __forceinline__ void slice_unit(const double (&v)[8], uint32_t E, int
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// named barriers over one role's threads; return 1 on every thread if pred holds on any
+__device__ __forceinline__ int slicers_any(int pred) {
+  int r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.or.pred q, 1, 256, p;\n selp.s32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"(pred)
+      : "memory");
+  return r;
+}
+__device__ __forceinline__ int drainers_any(int pred) {
+  int r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.or.pred q, 2, 128, p;\n selp.s32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"(pred)
+      : "memory");
+  return r;
+}
+__device__ __forceinline__ void drainers_sync() { asm volatile("bar.sync 2, 128;" ::: "memory"); }
+
+// bounded wait that also gives up as soon as another thread of the CTA has given up; sleep_ns
+// between polls for the roles that wait most of the time
+__device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile int* ab, int* err,
+                                        uint32_t sleep_ns = 0) {
+  for (uint32_t i = 0; i < kWaitPolls; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*ab) return false;
+    if (sleep_ns) __nanosleep(sleep_ns);
+  }
+  *ab = 1;
+  if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
+  return false;
+}
+
 template <int NP>
 __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p) {
-  const int chunk = blockIdx.x, nchunks = gridDim.x;
-  constexpr int BN = NP < 8 ? NP : 8;  // n per drain block
+  constexpr int BN = NP < 8 ? NP : 8;  // B columns per drain block
   constexpr int NB = NP / BN;          // drain blocks
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bar_tma = reinterpret_cast<uint64_t*>(smem);       // [4]
-  uint64_t* bar_mma = reinterpret_cast<uint64_t*>(smem + 32);  // [2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
-  int* EAc = reinterpret_cast<int*>(smem + 128);
-  int* EBc = EAc + 16;
-  int* EAw = EAc + 32;
-  int* EBw = EAc + 48;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);           // [MAXST] FP64 stage landed
+  uint64_t* empty = full + MAXST;                                // [MAXST] FP64 stage consumed
+  uint64_t* dfull = reinterpret_cast<uint64_t*>(smem + 64);      // [MAXDST] digit stage written
+  uint64_t* dempty = reinterpret_cast<uint64_t*>(smem + 96);     // [MAXDST] its MMAs completed
+  uint64_t* pdone = reinterpret_cast<uint64_t*>(smem + 128);     // [2] a period's MMAs completed
+  uint64_t* pfin = reinterpret_cast<uint64_t*>(smem + 144);      // [2] a period's record published
+  uint64_t* drained = reinterpret_cast<uint64_t*>(smem + 160);   // [2] a set's drain finished
+  uint64_t* bar_fin = reinterpret_cast<uint64_t*>(smem + 176);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 192);
+  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + 196);
+  volatile int* rinfo = reinterpret_cast<volatile int*>(smem + 208);  // [MAXDST] period | first << 30
+  volatile int* plast = reinterpret_cast<volatile int*>(smem + 224);  // [2] the period is the last
+  int* Ecur = reinterpret_cast<int*>(smem + 256);                      // [32] A columns, then B
+  int* pe = reinterpret_cast<int*>(smem + 384);                        // [2][32] a period's exponents
   int* S = reinterpret_cast<int*>(smem + HDR);
-  unsigned char* ring = smem + HDR + SBYTES;
-  const uint32_t stage_bytes = p.tile_a + p.tile_b;
-  unsigned char* dig = ring + (size_t)p.stages * stage_bytes;  // 1024-aligned by the host
-  auto digA = [&](int b) { return dig + (size_t)b * (p.dig_a + p.dig_b); };
-  auto digB = [&](int b) { return p.gram ? digA(b) : digA(b) + p.dig_a; };
-  auto tileA = [&](int s) { return reinterpret_cast<double*>(ring + (size_t)s * stage_bytes); };
-  auto tileB = [&](int s) {
-    return p.gram ? tileA(s) : reinterpret_cast<double*>(ring + (size_t)s * stage_bytes + p.tile_a);
-  };
+  double* cacc = reinterpret_cast<double*>(smem + HDR + SBYTES);
+  unsigned char* ring = smem + HDR + SBYTES + CBYTES;
+  unsigned char* dig = ring + (size_t)p.stages * p.stage_bytes;  // 1024-aligned by the host
+  auto digA = [&](int d) { return dig + (size_t)d * (p.dig_a + p.dig_b); };
+  auto digB = [&](int d) { return p.gram ? digA(d) : digA(d) + p.dig_a; };
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int M = p.M, N = p.N, MP = p.gram ? NP : p.MP;
-  const int RSW = p.sw * W;  // rows per super-window
-  const int64_t t_begin = p.ntiles * chunk / nchunks;
-  const int64_t t_end = p.ntiles * (chunk + 1) / nchunks;
+  const int M = p.M, N = p.N, MP = p.MP;
+  const int chunk = blockIdx.x, nchunks = gridDim.x;
+  const int64_t t_begin = p.nrounds * chunk / nchunks;
+  const int64_t t_end = p.nrounds * (chunk + 1) / nchunks;
   const int nt = (int)(t_end - t_begin);
-  auto is_bulk = [&](int64_t t) { return p.bulk && (t + 1) * (int64_t)RSW < p.K; };
-  auto issue = [&](int64_t t, int s) {
-    const int64_t r0 = t * RSW;
-    const uint32_t ba = (uint32_t)(RSW * p.lda * 8), bb = p.gram ? 0u : (uint32_t)(RSW * p.ldb * 8);
-    mbar_arrive_expect_tx(&bar_tma[s], ba + bb);
-    bulk_g2s(tileA(s), p.A + r0 * p.lda, ba, &bar_tma[s]);
-    if (!p.gram) bulk_g2s(tileB(s), p.B + r0 * p.ldb, bb, &bar_tma[s]);
-  };
+  const int DST = p.dstages;
+  // a round is bulk-copied when its rows end before the last row of the operand starts
+  auto is_bulk = [&](int64_t t) { return p.bulk && (t + 1) * (int64_t)p.rr < p.K; };
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -194,239 +250,291 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int s = 0; s < p.stages; s++) mbar_init(&bar_tma[s], 1);
-    mbar_init(&bar_mma[0], 1);
-    mbar_init(&bar_mma[1], 1);
+    for (int s = 0; s < p.stages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NSLICE);
+    }
+    for (int d = 0; d < DST; d++) {
+      mbar_init(&dfull[d], NSLICE);
+      mbar_init(&dempty[d], 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&pdone[i], 1);
+      mbar_init(&pfin[i], 1);
+      mbar_init(&drained[i], 1);
+    }
+    mbar_init(bar_fin, 1);
+    *abort_f = 0;
     fence_mbar_init();
   }
-  if (tid < 64) EAc[tid] = 0;  // EAc, EBc, EAw, EBw
+  if (tid < 32) Ecur[tid] = 0;
+  for (int e = tid; e < SBYTES / 4; e += THREADS) S[e] = 0;
+  for (int e = tid; e < CBYTES / 8; e += THREADS) cacc[e] = 0.0;
+  // padding rows of the digit stages stay zero: clear every stage once
+  for (uint32_t o = tid * 16; o < (uint32_t)DST * (p.dig_a + p.dig_b); o += THREADS * 16)
+    *reinterpret_cast<uint4*>(dig + o) = make_uint4(0, 0, 0, 0);
+  fence_proxy_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  if (p.bulk && tid == 0)
-    for (int i = 0; i < nt && i < p.stages; i++)
-      if (is_bulk(t_begin + i)) issue(t_begin + i, i);
 
-  // idesc: D f32, A/B f16, K-major both, N = nmma, M = 128
-  const uint32_t idesc = (1u << 4) | ((uint32_t)(p.nmma >> 3) << 17) | ((128u >> 4) << 24);
-
-  // Slicing units: (operand, column c, k-octet o).  A units u < nA: c = u % MP, o = u / MP;
-  // B units nA <= u < nA + nB: c = (u - nA) % NP.  nA is a multiple of 32, so a warp holds units
-  // of one operand and lanes with equal c sit at xor distances that are multiples of MP (NP).
-  const int nA = p.sw * OCT * MP;
-  const int nA_al = (nA + 31) & ~31;  // B units start on a warp boundary
-  const int nB = p.gram ? 0 : p.sw * OCT * NP;
-  const int nU = nA_al + nB;          // <= 2 * THREADS (host guarantees)
-  const int u0 = tid, u1 = tid + THREADS;
-  double cacc = 0.0;  // FP64 accumulator of C entry tid (tid < M*N), CTA-local
-  int uses[2] = {0, 0};
-  int period_rows = 0;
-  bool active = false;
-  bool bail = false;
-
-  // ---- drain: TMEM -> level sums -> FP64 accumulators -------------------------------------------
-  auto drain = [&]() {
-    for (int e = tid; e < 8 * 16 * 16; e += THREADS) S[e] = 0;
-    __syncthreads();
-    tc_fence_after();
-    const int q = warp & 3, half = warp >> 2;
-    const int r = 32 * q + lane;  // TMEM lane = A digit row
-    const int i0 = r / MP, m = r - i0 * MP;  // digit index (0-based) and column of A
-    const bool rvalid = (i0 < DIGITS) && (m < M);
-    for (int nb = half; nb < NB; nb += 2) {
-      uint32_t raw[DIGITS][BN];
-#pragma unroll
-      for (int j = 0; j < DIGITS; j++) {
-        uint32_t tmp[BN];
-        tmem_ld<BN>(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(j * NP + nb * BN), tmp);
-#pragma unroll
-        for (int x = 0; x < BN; x++) raw[j][x] = tmp[x];
+  if (warp == WPROD) {
+    // ---- producer: whole rounds of rows of A and B into the FP64 stage ring ----------------------
+    int issued = 0;
+    for (int t = 0; t < nt; t++) {
+      const int s = t % p.stages, use = t / p.stages;
+      if (use > 0) {
+        int ok = 0;
+        if (lane == 0) ok = wait_ab(&empty[s], (uint32_t)((use - 1) & 1), abort_f, p.err, SLEEP_PRODUCER);
+        if (!__shfl_sync(0xffffffffu, ok, 0)) break;
       }
-      tmem_wait_ld();
-#pragma unroll
-      for (int x = 0; x < BN; x++) {
-        const int n = nb * BN + x;
-        int R[DIGITS];
-#pragma unroll
-        for (int j = 0; j < DIGITS; j++) R[j] = rvalid ? __float2int_rn(__uint_as_float(raw[j][x])) : 0;
-        // rotate so that R[t] holds the pair (i0+1, j) of level t+2, i.e. j-1 = t - i0
-#pragma unroll
-        for (int b = 1; b < DIGITS; b <<= 1) {
-          if (i0 & b) {
-            int T[DIGITS];
-#pragma unroll
-            for (int t = 0; t < DIGITS; t++) T[t] = R[(t - b + DIGITS) % DIGITS];
-#pragma unroll
-            for (int t = 0; t < DIGITS; t++) R[t] = T[t];
-          }
-        }
-#pragma unroll
-        for (int t = 0; t < DIGITS; t++) {
-          int c = (i0 <= t) ? R[t] : 0;
-          for (int o = MP; o < 32; o <<= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-          if (lane < MP && rvalid && n < N) atomicAdd(&S[(t * 16 + m) * 16 + n], c);
+      if (lane == 0) {
+        const int64_t tt = t_begin + t;
+        if (is_bulk(tt)) {
+          const int64_t r0 = tt * p.rr;
+          const uint32_t ba = (uint32_t)(p.rr * p.lda * 8), bb = p.gram ? 0u : (uint32_t)(p.rr * p.ldb * 8);
+          unsigned char* st = ring + (size_t)s * p.stage_bytes;
+          mbar_arrive_expect_tx(&full[s], ba + bb);
+          bulk_g2s(st, p.A + r0 * p.lda, ba, &full[s]);
+          if (!p.gram) bulk_g2s(st + p.tile_a, p.B + r0 * p.ldb, bb, &full[s]);
+        } else {
+          mbar_arrive(&full[s]);  // no copy: the slicers read this round from global memory
         }
       }
+      issued = t + 1;
     }
-    tc_fence_before();
-    __syncthreads();
-    if (tid < M * N) {
-      const int mm = tid % M, nn = tid / M;
-      long long s[8];
-#pragma unroll
-      for (int t = 0; t < 8; t++) s[t] = S[(t * 16 + mm) * 16 + nn];
-      const long long vhi = (s[0] << 24) + (s[1] << 16) + (s[2] << 8) + s[3];
-      const long long vlo = (s[4] << 24) + (s[5] << 16) + (s[6] << 8) + s[7];
-      const int ea = EAc[mm], eb = p.gram ? EAc[nn] : EBc[nn];
-      const double v = fma((double)vlo, 0x1p-32, (double)vhi);  // in units of 2^(EA+EB-2080)
-      cacc = fma(v * pow2i(ea - 1040), pow2i(eb - 1040), cacc);
-    }
-  };
-
-  auto unit_info = [&](int u, bool& isA, int& c, int& o, bool& valid) {
-    isA = u < nA_al;
-    const int v = isA ? u : u - nA_al;
-    const int CP = isA ? MP : NP;
-    c = v % CP;
-    o = v / CP;
-    valid = (isA ? v < nA : v < nB) && c < (isA ? M : N);
-  };
-
-  for (int it = 0; it < nt && !bail; it++) {
-    const int64_t t = t_begin + it;
-    const int s = it % p.stages;
-    const int64_t r0 = t * RSW;
-    const int rows = (int)((p.K - r0) < RSW ? (p.K - r0) : RSW);
-    double* TA = tileA(s);
-    double* TB = tileB(s);
-    if (is_bulk(t)) {
-      bool ok = mbar_wait_bounded(&bar_tma[s], (uint32_t)((it / p.stages) & 1), p.err);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
-        break;
-      }
-    } else {
-      for (int e = tid; e < rows * M; e += THREADS) {
-        int rr = e / M, c = e - rr * M;
-        TA[rr * p.lda_s + c] = p.A[(r0 + rr) * p.lda + c];
-      }
-      if (!p.gram)
-        for (int e = tid; e < rows * N; e += THREADS) {
-          int rr = e / N, c = e - rr * N;
-          TB[rr * p.ldb_s + c] = p.B[(r0 + rr) * p.ldb + c];
-        }
-      __syncthreads();
-    }
-    // load my (up to two) units and reduce the super-window's exponent maxima
-    double v[2][8];
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const int u = k ? u1 : u0;
-      bool isA, valid;
-      int c, o;
-      unit_info(u, isA, c, o, valid);
-      const double* T = isA ? TA : TB;
-      const int64_t ld = isA ? p.lda_s : p.ldb_s;
-      uint32_t e = 0;
-#pragma unroll
-      for (int q2 = 0; q2 < 8; q2++) {
-        const int rr = o * 8 + q2;
-        v[k][q2] = (valid && rr < rows) ? T[rr * ld + c] : 0.0;
-        e = max(e, exp_field(v[k][q2]));
-      }
-      if (u - lane < nU) {  // warp-uniform: the warp holds units
-        const int CP = isA ? MP : NP;
-        for (int x = CP; x < 32; x <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, x));
-        if (lane < CP && valid && e) atomicMax(isA ? &EAw[c] : &EBw[c], (int)e);
-      }
-    }
-    __syncthreads();
-    bool need = !active || period_rows + RSW > PERIOD;
-    if (tid < M && EAw[tid] > EAc[tid]) need = true;
-    if (!p.gram && tid < N && EBw[tid] > EBc[tid]) need = true;
-    if (__syncthreads_or(need)) {
-      if (active) {
-        const int bl = (it - 1) & 1;
-        bool ok = mbar_wait_bounded(&bar_mma[bl], (uint32_t)((uses[bl] - 1) & 1), p.err);
-        if (__syncthreads_or(!ok)) {
-          bail = true;
+    // copies in flight land before the CTA ends
+    if (lane == 0)
+      for (int t = max(0, issued - p.stages); t < issued; t++)
+        mbar_wait_bounded(&full[t % p.stages], (uint32_t)((t / p.stages) & 1), nullptr);
+  } else if (warp == WMMA) {
+    // ---- MMA issuer -------------------------------------------------------------------------------
+    if (lane == 0) {
+      // idesc: D f32, A/B f16, K-major both, N = nmma, M = 128
+      const uint32_t idesc = (1u << 4) | ((uint32_t)(p.nmma >> 3) << 17) | ((128u >> 4) << 24);
+      const uint32_t lbb = p.gram ? p.lbo_a : p.lbo_b;
+      int pcur = -1, issued = 0;
+      bool ok = true;
+      for (int t = 0; t < nt; t++) {
+        const int d = t % DST;
+        if (!wait_ab(&dfull[d], (uint32_t)((t / DST) & 1), abort_f, p.err, SLEEP_MMA)) {
+          ok = false;
           break;
         }
-        drain();
+        tc_fence_after();
+        const int info = rinfo[d];
+        const int pp = info & 0x3FFFFFFF;
+        const bool first = (info >> 30) & 1;
+        if (first) {
+          if (pp >= 1) {  // the previous period is complete once its MMAs finish
+            mma_commit(&pdone[(pp - 1) & 1]);
+            plast[(pp - 1) & 1] = 0;
+            mbar_arrive(&pfin[(pp - 1) & 1]);
+          }
+          if (pp >= 2) {  // this period's accumulator set was drained (period pp - 2)
+            if (!wait_ab(&drained[pp & 1], (uint32_t)(((pp - 2) >> 1) & 1), abort_f, p.err, SLEEP_MMA)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+          }
+        }
+        const uint32_t a0 = smem_u32(digA(d)), b0 = smem_u32(digB(d));
+        const uint32_t dcol = tmem + (uint32_t)((pp & 1) * p.nmma);
+        const int ksteps = p.rr / 16;
+        for (int ks = 0; ks < ksteps; ks++)
+          mma_f16(dcol, make_desc(a0 + 2 * ks * p.lbo_a, p.lbo_a), make_desc(b0 + 2 * ks * lbb, lbb), idesc,
+                   (first && ks == 0) ? 0u : 1u);
+        mma_commit(&dempty[d]);
+        pcur = pp;
+        issued++;
       }
-      __syncthreads();
-      if (tid < M) EAc[tid] = max(EAc[tid], EAw[tid]);
-      if (!p.gram && tid < N) EBc[tid] = max(EBc[tid], EBw[tid]);
-      period_rows = 0;
-      __syncthreads();
-    }
-    const int b = it & 1;
-    if (uses[b] > 0) {
-      bool ok = mbar_wait_bounded(&bar_mma[b], (uint32_t)((uses[b] - 1) & 1), p.err);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
-        break;
+      if (ok && pcur >= 0) {
+        mma_commit(&pdone[pcur & 1]);
+        plast[pcur & 1] = 1;
+        mbar_arrive(&pfin[pcur & 1]);
+      }
+      if (issued) {  // every MMA has finished before the TMEM is released
+        mma_commit(bar_fin);
+        mbar_wait_bounded(bar_fin, 0, nullptr);
       }
     }
+  } else if (warp >= NSLICE) {
+    // ---- drain: a period's TMEM set -> level sums -> FP64 accumulators ---------------------------
+    const int q = warp - NSLICE;        // TMEM lane quadrant
+    const int dtid = tid - SLICERS;     // 0..127
+    const int r = 32 * q + lane;        // TMEM lane = A digit row
+    const int i0 = r / MP, m = r - i0 * MP;  // digit index (0-based) and column of A
+    const bool rvalid = (i0 < DIGITS) && (m < M);
+    for (int pp = 0; nt > 0; pp++) {  // K = 0: no rounds, no periods
+      const int set = pp & 1;
+      const uint32_t par = (uint32_t)((pp >> 1) & 1);
+      // one lane per warp polls (sleeping in between); the warp follows
+      int ok = 1;
+      if (lane == 0) {
+        ok = wait_ab(&pfin[set], par, abort_f, p.err, SLEEP_DRAIN);
+        if (ok) ok = wait_ab(&pdone[set], par, abort_f, p.err, SLEEP_DRAIN);
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (drainers_any(!ok)) break;
+      tc_fence_after();
+      const bool last = plast[set] != 0;
+      for (int nb = 0; nb < NB; nb++) {
+        uint32_t raw[DIGITS][BN];
+#pragma unroll
+        for (int j = 0; j < DIGITS; j++) {
+          uint32_t tmp[BN];
+          tmem_ld<BN>(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(set * p.nmma + j * NP + nb * BN), tmp);
+#pragma unroll
+          for (int x = 0; x < BN; x++) raw[j][x] = tmp[x];
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int x = 0; x < BN; x++) {
+          const int n = nb * BN + x;
+          int R[DIGITS];
+#pragma unroll
+          for (int j = 0; j < DIGITS; j++) R[j] = rvalid ? __float2int_rn(__uint_as_float(raw[j][x])) : 0;
+          // rotate so that R[t] holds the pair (i0+1, j) of level t+2, i.e. j-1 = t - i0
+#pragma unroll
+          for (int b = 1; b < DIGITS; b <<= 1) {
+            if (i0 & b) {
+              int T[DIGITS];
+#pragma unroll
+              for (int t = 0; t < DIGITS; t++) T[t] = R[(t - b + DIGITS) % DIGITS];
+#pragma unroll
+              for (int t = 0; t < DIGITS; t++) R[t] = T[t];
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < DIGITS; t++) {
+            int c = (i0 <= t) ? R[t] : 0;
+            for (int o = MP; o < 32; o <<= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+            if (lane < MP && rvalid && n < N) atomicAdd(&S[(t * 16 + m) * 16 + n], c);
+          }
+        }
+      }
+      tc_fence_before();
+      drainers_sync();
+      for (int e = dtid; e < M * N; e += NDRAIN * 32) {
+        const int mm = e % M, nn = e / M;
+        long long sv[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) sv[t] = S[(t * 16 + mm) * 16 + nn];
+        const long long vhi = (sv[0] << 24) + (sv[1] << 16) + (sv[2] << 8) + sv[3];
+        const long long vlo = (sv[4] << 24) + (sv[5] << 16) + (sv[6] << 8) + sv[7];
+        const int ea = pe[set * 32 + mm], eb = pe[set * 32 + (p.gram ? nn : 16 + nn)];
+        const double v = fma((double)vlo, 0x1p-32, (double)vhi);  // in units of 2^(EA+EB-2080)
+        cacc[e] = fma(v * pow2i(ea - 1040), pow2i(eb - 1040), cacc[e]);
+      }
+      drainers_sync();
+      for (int e = dtid; e < SBYTES / 4; e += NDRAIN * 32) S[e] = 0;  // before the next period's atomics
+      if (dtid == 0) mbar_arrive(&drained[set]);
+      if (last) break;
+    }
+  } else {
+    // ---- slicers: one unit = one column and 8 rows; A units first, then B units ------------------
+    const int NUA = (p.rr / 8) * MP;
+    const int NUB = p.gram ? 0 : (p.rr / 8) * NP;
+    const int NU = NUA + NUB;  // <= 2 * SLICERS (host guarantees)
+    int ucol[2], uoct[2], uop[2];
+    bool uval[2];
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const int u = k ? u1 : u0;
-      bool isA, valid;
-      int c, o;
-      unit_info(u, isA, c, o, valid);
-      if (valid) {
-        if (isA)
-          slice_unit(v[k], (uint32_t)EAc[c], c, MP, o, p.lbo_a, digA(b));
-        else
-          slice_unit(v[k], (uint32_t)EBc[c], c, NP, o, p.lbo_b, digB(b));
+      const int u = tid + k * SLICERS;
+      if (u < NUA) {
+        uop[k] = 0;
+        ucol[k] = u % MP;
+        uoct[k] = u / MP;
+        uval[k] = ucol[k] < M;
+      } else {
+        const int v = u - NUA;
+        uop[k] = 1;
+        ucol[k] = v % NP;
+        uoct[k] = v / NP;
+        uval[k] = u < NU && ucol[k] < N;
       }
     }
-    if (tid < 16) EAw[tid] = 0;
-    else if (tid < 32) EBw[tid - 16] = 0;
-    fence_proxy_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(digA(b)), b0 = smem_u32(digB(b));
-      const uint32_t lbb = p.gram ? p.lbo_a : p.lbo_b;
-      const int ksteps = RSW / 16;
-      for (int ks = 0; ks < ksteps; ks++)
-        mma_f16(tmem, make_desc(a0 + 2 * ks * p.lbo_a, p.lbo_a), make_desc(b0 + 2 * ks * lbb, lbb), idesc,
-                 (period_rows > 0 || ks > 0) ? 1u : 0u);
-      mma_commit(&bar_mma[b]);
-      if (p.bulk && it + p.stages < nt && is_bulk(t + p.stages)) {
+    int Ereg[2] = {0, 0};
+    int pp = -1, period_rows = 0;
+    for (int t = 0; t < nt; t++) {
+      const int s = t % p.stages, d = t % DST;
+      const int64_t tt = t_begin + t;
+      const int64_t r0 = tt * p.rr;
+      const int rows = (int)((p.K - r0) < p.rr ? (p.K - r0) : p.rr);
+      const bool ok = wait_ab(&full[s], (uint32_t)((t / p.stages) & 1), abort_f, p.err);
+      const bool blk = is_bulk(tt);
+      const double* stA = reinterpret_cast<const double*>(ring + (size_t)s * p.stage_bytes);
+      const double* stB = p.gram ? stA : reinterpret_cast<const double*>(ring + (size_t)s * p.stage_bytes + p.tile_a);
+      double v[2][8];
+      uint32_t eu[2] = {0u, 0u};
+      bool exceed = false;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const bool isB = uop[k] != 0;
+        const int64_t ld = isB ? p.ldb : p.lda;
+        const double* src = blk ? (isB ? stB : stA) : ((isB ? p.B : p.A) + r0 * ld);
+#pragma unroll
+        for (int q2 = 0; q2 < 8; q2++) {
+          const int rr = uoct[k] * 8 + q2;
+          v[k][q2] = (ok && uval[k] && rr < rows) ? src[rr * ld + ucol[k]] : 0.0;
+          eu[k] = max(eu[k], exp_field(v[k][q2]));
+        }
+        if (uval[k] && (int)eu[k] > Ereg[k]) exceed = true;
+      }
+      const bool newp = pp < 0 || period_rows + p.rr > PERIOD || exceed;
+      bool first = false;
+      if (slicers_any(!ok || newp)) {
+        if (slicers_any(!ok)) break;
+        // a new period: raise the exponents of the columns that met larger elements
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+          if (uval[k] && (int)eu[k] > Ereg[k]) atomicMax(&Ecur[uop[k] * 16 + ucol[k]], (int)eu[k] + HEAD);
+        pp++;
+        bool ok2 = true;  // the period's exponent slot and accumulator set held period pp - 2
+        if (pp >= 2) ok2 = wait_ab(&drained[pp & 1], (uint32_t)(((pp - 2) >> 1) & 1), abort_f, p.err);
+        if (slicers_any(!ok2)) break;  // also orders the atomics before the reads below
+        if (tid < 32) pe[(pp & 1) * 32 + tid] = Ecur[tid];
+#pragma unroll
+        for (int k = 0; k < 2; k++) Ereg[k] = uval[k] ? Ecur[uop[k] * 16 + ucol[k]] : 0;
+        period_rows = 0;
+        first = true;
+      }
+      // the FP64 stage is consumed: the values are in registers
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      int okd = 1;  // the digit stage is free once the MMAs of round t - DST completed
+      if (t >= DST) {
+        if (lane == 0) okd = wait_ab(&dempty[d], (uint32_t)(((t / DST) - 1) & 1), abort_f, p.err);
+        okd = __shfl_sync(0xffffffffu, okd, 0);
+      }
+      if (okd) {
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+          if (uval[k]) {
+            if (uop[k])
+              slice_unit(v[k], (uint32_t)Ereg[k], ucol[k], NP, uoct[k], p.lbo_b, digB(d));
+            else
+              slice_unit(v[k], (uint32_t)Ereg[k], ucol[k], MP, uoct[k], p.lbo_a, digA(d));
+          }
+        if (tid == 0) rinfo[d] = pp | (first ? (1 << 30) : 0);
         fence_proxy_async_smem();
-        issue(t + p.stages, s);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&dfull[d]);
       }
+      period_rows += p.rr;
     }
-    uses[b]++;
-    period_rows += RSW;
-    active = true;
   }
 
-  if (!bail && active) {
-    const int bl = (nt - 1) & 1;
-    bool ok = mbar_wait_bounded(&bar_mma[bl], (uint32_t)((uses[bl] - 1) & 1), p.err);
-    if (__syncthreads_or(!ok))
-      bail = true;
-    else
-      drain();
-  }
-  if (bail) {
-    // let MMAs already issued finish before the TMEM is released (bounded)
-    for (int bb = 0; bb < 2; bb++)
-      if (uses[bb] > 0) mbar_wait_bounded(&bar_mma[bb], (uint32_t)((uses[bb] - 1) & 1), nullptr);
-  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols));
-  if (bail) return;
+  if (*abort_f) return;  // timeout recorded in the error word; no partial, no ticket
 
   // ---- cross-CTA finish -----------------------------------------------------------------------
   const int MN = M * N;
-  if (tid < MN) p.partials[(size_t)chunk * MN + tid] = cacc;
+  if (tid < MN) p.partials[(size_t)chunk * MN + tid] = cacc[tid];
   __threadfence();
   __syncthreads();
   __shared__ int s_last;
@@ -437,10 +545,9 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
   double* red = reinterpret_cast<double*>(ring);
   const int P = THREADS / MN;  // >= 1 since MN <= 256
   const int e = tid % MN, j = tid / MN;
-  const int nb = nchunks;
   if (j < P) {
     double sum = 0.0;
-    const int b0 = (int)((int64_t)nb * j / P), b1 = (int)((int64_t)nb * (j + 1) / P);
+    const int b0 = (int)((int64_t)nchunks * j / P), b1 = (int)((int64_t)nchunks * (j + 1) / P);
     for (int bb = b0; bb < b1; bb++) sum += __ldcg(&p.partials[(size_t)bb * MN + e]);
     red[j * MN + e] = sum;
   }
@@ -516,56 +623,54 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.gram = (A == B) && (lda == ldb) && (M == N);
   const int NP = pow2ceil(a.gram ? M : N);
   a.MP = a.gram ? NP : pow2ceil(M);
-  // windows per iteration: the largest power of two (<= PERIOD / W) whose slicing units
-  // (k-octet x column; A units padded to a warp multiple) fit two per thread
-  auto units = [&](int w) {
-    return (int)round_up((int64_t)w * OCT * a.MP, 32) + (a.gram ? 0 : w * OCT * NP);
-  };
-  int sw = PERIOD / W;
-  while (sw > 1 && units(sw) > 2 * THREADS) sw >>= 1;
-  if (units(sw) > 2 * THREADS) {
+  a.NP = NP;
+  // rows per round: 128 * R with R the largest power of two whose slicing units (one column and
+  // 8 rows each) fit two per slicer thread (a round's fixed costs -- the slicers' barrier, the
+  // hand-offs, the MMA commit -- then spread over more rows)
+  const int cols = a.MP + (a.gram ? 0 : NP);
+  int R = 1;
+  while (R < PERIOD / 128 && 2 * R * 16 * cols <= 2 * SLICERS) R *= 2;
+  a.rr = 128 * R;
+  if ((a.rr / 8) * cols > 2 * SLICERS) {
     set_error("split precision: too many slicing units");
     return SKINNY_UNSUPPORTED;
   }
-  a.sw = sw;
-  const int64_t RSW = (int64_t)sw * W;
-  const bool aligned = ((uintptr_t)A % 16 == 0) && (a.gram || (uintptr_t)B % 16 == 0);
-  const bool dense = lda <= 2 * M + 16 && (a.gram || ldb <= 2 * N + 16);
   a.nmma = std::max(16, 8 * NP);
-  a.tmem_cols = a.nmma <= 32 ? 32 : (a.nmma <= 64 ? 64 : 128);
+  a.tmem_cols = std::max(32, 2 * a.nmma);
   a.lbo_a = (uint32_t)(8 * a.MP * 16);
   a.lbo_b = (uint32_t)(a.nmma * 16);
-  const int64_t octs = (int64_t)sw * OCT;
+  const int64_t octs = a.rr / 8;
   a.dig_a = (uint32_t)round_up(octs * a.lbo_a + DPAD, 1024);
   a.dig_b = a.gram ? 0u : (uint32_t)round_up(octs * a.lbo_b, 1024);
-  const int64_t dig = (int64_t)2 * (a.dig_a + a.dig_b);
-  const int64_t fixed = HDR + SBYTES + dig;
-  // FP64 stages: whole (padded) rows by bulk copy where they fit two stages, else the M (N) used
-  // columns by plain loads
-  int64_t stage = 0;
-  int stages = 0;
-  for (int bulk = (aligned && dense && K > RSW) ? 1 : 0; bulk >= 0; bulk--) {
+  // a round starts at a multiple of 128 rows, so its bytes start 16-byte aligned with the operand
+  const bool aligned = ((uintptr_t)A % 16 == 0) && (a.gram || (uintptr_t)B % 16 == 0);
+  const bool dense = lda <= 2 * M + 16 && (a.gram || ldb <= 2 * N + 16);
+  a.tile_a = (uint32_t)round_up((int64_t)a.rr * lda * 8, 128);
+  const int64_t tile_b = a.gram ? 0 : round_up((int64_t)a.rr * ldb * 8, 128);
+  // FP64 stages and digit stages: the deepest rings that fit (at least two of each); bulk copies
+  // of whole rounds where aligned dense rows fit, else the slicers read global memory
+  const int64_t fixed = HDR + SBYTES + CBYTES + STATIC_RESERVE;
+  const int64_t dstage = (int64_t)a.dig_a + a.dig_b;
+  a.stages = 0;
+  for (int bulk = (aligned && dense && K > a.rr) ? 1 : 0; bulk >= 0 && a.stages == 0; bulk--) {
     a.bulk = bulk;
-    a.lda_s = a.bulk ? lda : M;
-    a.ldb_s = a.gram ? a.lda_s : (a.bulk ? ldb : N);
-    a.tile_a = (uint32_t)round_up(RSW * a.lda_s * 8, 128);
-    a.tile_b = a.gram ? 0u : (uint32_t)round_up(RSW * a.ldb_s * 8, 128);
-    stage = round_up(a.tile_a + a.tile_b, 1024);
-    stages = (int)std::min<int64_t>(4, (h->dev.smem_optin - fixed) / stage);
-    if (stages >= 2) break;
+    a.stage_bytes = bulk ? (uint32_t)round_up(a.tile_a + tile_b, 1024) : 1024u;
+    for (int dst = MAXDST; dst >= 2 && a.stages == 0; dst--)
+      for (int nst = MAXST; nst >= 2; nst--)
+        if (fixed + (int64_t)nst * a.stage_bytes + (int64_t)dst * dstage <= h->dev.smem_optin) {
+          a.stages = nst;
+          a.dstages = dst;
+          break;
+        }
   }
-  if (a.gram)
-    a.tile_a = (uint32_t)stage;
-  else
-    a.tile_b = (uint32_t)(stage - a.tile_a);
-  if (stages < 2) {
-    set_error("split precision: tiles do not fit in shared memory");
+  if (a.stages == 0) {
+    set_error("split precision: stages do not fit in shared memory");
     return SKINNY_UNSUPPORTED;
   }
-  a.stages = stages;
-  a.ntiles = (K + RSW - 1) / RSW;
-  const int smem2 = (int)(fixed + stages * stage);
-  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(a.ntiles, h->dev.sms));
+  a.nrounds = (K + a.rr - 1) / a.rr;
+  const int smem2 =
+      (int)(fixed - STATIC_RESERVE + (int64_t)a.stages * a.stage_bytes + (int64_t)a.dstages * dstage);
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(a.nrounds, h->dev.sms));
   Workspace& ws = h->ws[st];
   skinny_status s = workspace_ensure(ws, (size_t)grid * M * N * 8, st);
   if (s != SKINNY_OK) return s;

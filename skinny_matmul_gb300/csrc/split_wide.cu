@@ -141,11 +141,14 @@ __device__ __forceinline__ int slicers_any(int pred) {
 }
 __device__ __forceinline__ void slicers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// bounded wait that also gives up as soon as another thread of the CTA has given up
-__device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile int* ab, int* err) {
+// bounded wait that also gives up as soon as another thread of the CTA has given up; the producer
+// and MMA warps sleep between polls so that their polling leaves issue slots to the slicers
+__device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile int* ab, int* err,
+                                        uint32_t sleep_ns = 0) {
   for (uint32_t i = 0; i < (1u << 22); i++) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*ab) return false;
+    if (sleep_ns) __nanosleep(sleep_ns);
   }
   *ab = 1;
   if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       const int rs = ls % R, use = ls / R;
       if (use > 0) {
         int ok = 0;
-        if (lane == 0) ok = wait_ab(&raw_empty[rs], (uint32_t)((use - 1) & 1), abort_f, p.err);
+        if (lane == 0) ok = wait_ab(&raw_empty[rs], (uint32_t)((use - 1) & 1), abort_f, p.err, 64);
         if (!__shfl_sync(0xffffffffu, ok, 0)) break;
       }
       const int64_t row0 = (s_begin + ls) * ROWS;
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       int issued = 0;
       for (int ls = 0; ls < nst; ls++) {
         const int ds = ls % DSLOTS;
-        if (!wait_ab(&dfull[ds], (uint32_t)((ls / DSLOTS) & 1), abort_f, p.err)) break;
+        if (!wait_ab(&dfull[ds], (uint32_t)((ls / DSLOTS) & 1), abort_f, p.err, 32)) break;
         tc_after();
         const int f = flags[ds];
         const uint32_t start = f & 1, buf = (f >> 1) & 1;
