@@ -470,17 +470,31 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
       double v[2][8];
       uint32_t eu[2] = {0u, 0u};
       bool exceed = false;
+      // The 8 rows of an octet o are visited in the order q ^ (o & 7), the same for A and B (a
+      // permutation of k inside a k-octet leaves the MMA's sum unchanged): lanes of a half-warp
+      // holding different octets then read different banks of the FP64 stage.
 #pragma unroll
       for (int k = 0; k < 2; k++) {
         const bool isB = uop[k] != 0;
         const int64_t ld = isB ? p.ldb : p.lda;
-        const double* src = blk ? (isB ? stB : stA) : ((isB ? p.B : p.A) + r0 * ld);
+        const int g = uoct[k] & 7;
+        if (blk) {  // shared-memory stage
+          const double* src = isB ? stB : stA;
 #pragma unroll
-        for (int q2 = 0; q2 < 8; q2++) {
-          const int rr = uoct[k] * 8 + q2;
-          v[k][q2] = (ok && uval[k] && rr < rows) ? src[rr * ld + ucol[k]] : 0.0;
-          eu[k] = max(eu[k], exp_field(v[k][q2]));
+          for (int q2 = 0; q2 < 8; q2++) {
+            const int rr = uoct[k] * 8 + (q2 ^ g);
+            v[k][q2] = (ok && uval[k]) ? src[rr * ld + ucol[k]] : 0.0;
+          }
+        } else {  // global memory (rows not 16-byte aligned, or the last round)
+          const double* src = (isB ? p.B : p.A) + r0 * ld;
+#pragma unroll
+          for (int q2 = 0; q2 < 8; q2++) {
+            const int rr = uoct[k] * 8 + (q2 ^ g);
+            v[k][q2] = (ok && uval[k] && rr < rows) ? src[rr * ld + ucol[k]] : 0.0;
+          }
         }
+#pragma unroll
+        for (int q2 = 0; q2 < 8; q2++) eu[k] = max(eu[k], exp_field(v[k][q2]));
         if (uval[k] && (int)eu[k] > Ereg[k]) exceed = true;
       }
       const bool newp = pp < 0 || period_rows + p.rr > PERIOD || exceed;
@@ -625,43 +639,41 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.MP = a.gram ? NP : pow2ceil(M);
   a.NP = NP;
   // rows per round: 128 * R with R the largest power of two whose slicing units (one column and
-  // 8 rows each) fit two per slicer thread (a round's fixed costs -- the slicers' barrier, the
-  // hand-offs, the MMA commit -- then spread over more rows)
+  // 8 rows each) fit two per slicer thread and whose FP64 and digit stages fit in shared memory
+  // (at least two of each; bulk copies of whole rounds where aligned dense rows fit, else the
+  // slicers read global memory).  A round's fixed costs -- the slicers' barrier, the hand-offs,
+  // the MMA commit -- then spread over as many rows as possible.
   const int cols = a.MP + (a.gram ? 0 : NP);
-  int R = 1;
-  while (R < PERIOD / 128 && 2 * R * 16 * cols <= 2 * SLICERS) R *= 2;
-  a.rr = 128 * R;
-  if ((a.rr / 8) * cols > 2 * SLICERS) {
-    set_error("split precision: too many slicing units");
-    return SKINNY_UNSUPPORTED;
-  }
   a.nmma = std::max(16, 8 * NP);
   a.tmem_cols = std::max(32, 2 * a.nmma);
   a.lbo_a = (uint32_t)(8 * a.MP * 16);
   a.lbo_b = (uint32_t)(a.nmma * 16);
-  const int64_t octs = a.rr / 8;
-  a.dig_a = (uint32_t)round_up(octs * a.lbo_a + DPAD, 1024);
-  a.dig_b = a.gram ? 0u : (uint32_t)round_up(octs * a.lbo_b, 1024);
   // a round starts at a multiple of 128 rows, so its bytes start 16-byte aligned with the operand
   const bool aligned = ((uintptr_t)A % 16 == 0) && (a.gram || (uintptr_t)B % 16 == 0);
   const bool dense = lda <= 2 * M + 16 && (a.gram || ldb <= 2 * N + 16);
-  a.tile_a = (uint32_t)round_up((int64_t)a.rr * lda * 8, 128);
-  const int64_t tile_b = a.gram ? 0 : round_up((int64_t)a.rr * ldb * 8, 128);
-  // FP64 stages and digit stages: the deepest rings that fit (at least two of each); bulk copies
-  // of whole rounds where aligned dense rows fit, else the slicers read global memory
   const int64_t fixed = HDR + SBYTES + CBYTES + STATIC_RESERVE;
-  const int64_t dstage = (int64_t)a.dig_a + a.dig_b;
+  int64_t dstage = 0;
   a.stages = 0;
-  for (int bulk = (aligned && dense && K > a.rr) ? 1 : 0; bulk >= 0 && a.stages == 0; bulk--) {
-    a.bulk = bulk;
-    a.stage_bytes = bulk ? (uint32_t)round_up(a.tile_a + tile_b, 1024) : 1024u;
-    for (int dst = MAXDST; dst >= 2 && a.stages == 0; dst--)
-      for (int nst = MAXST; nst >= 2; nst--)
-        if (fixed + (int64_t)nst * a.stage_bytes + (int64_t)dst * dstage <= h->dev.smem_optin) {
-          a.stages = nst;
-          a.dstages = dst;
-          break;
-        }
+  for (int R = PERIOD / 128; R >= 1 && a.stages == 0; R /= 2) {
+    if (R * 16 * cols > 2 * SLICERS) continue;
+    a.rr = 128 * R;
+    const int64_t octs = a.rr / 8;
+    a.dig_a = (uint32_t)round_up(octs * a.lbo_a + DPAD, 1024);
+    a.dig_b = a.gram ? 0u : (uint32_t)round_up(octs * a.lbo_b, 1024);
+    a.tile_a = (uint32_t)round_up((int64_t)a.rr * lda * 8, 128);
+    const int64_t tile_b = a.gram ? 0 : round_up((int64_t)a.rr * ldb * 8, 128);
+    dstage = (int64_t)a.dig_a + a.dig_b;
+    for (int bulk = (aligned && dense && K > a.rr) ? 1 : 0; bulk >= 0 && a.stages == 0; bulk--) {
+      a.bulk = bulk;
+      a.stage_bytes = bulk ? (uint32_t)round_up(a.tile_a + tile_b, 1024) : 1024u;
+      for (int dst = MAXDST; dst >= 2 && a.stages == 0; dst--)
+        for (int nst = MAXST; nst >= 2; nst--)
+          if (fixed + (int64_t)nst * a.stage_bytes + (int64_t)dst * dstage <= h->dev.smem_optin) {
+            a.stages = nst;
+            a.dstages = dst;
+            break;
+          }
+    }
   }
   if (a.stages == 0) {
     set_error("split precision: stages do not fit in shared memory");
