@@ -380,7 +380,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
       if (drainers_any(!ok)) break;
       tc_fence_after();
       const bool last = plast[set] != 0;
-      for (int nb = 0; nb < NB; nb++) {
+      // quadrants holding no digit row (8 * MP <= 32 q) have nothing to drain
+      for (int nb = 0; nb < (32 * q < DIGITS * MP ? NB : 0); nb++) {
         uint32_t raw[DIGITS][BN];
 #pragma unroll
         for (int j = 0; j < DIGITS; j++) {
@@ -395,6 +396,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
           const int n = nb * BN + x;
           int R[DIGITS];
 #pragma unroll
+          // exact (|sum| <= 2^24); the conversion pipe is otherwise idle, the ALU pipe is the slicers'
           for (int j = 0; j < DIGITS; j++) R[j] = rvalid ? __float2int_rn(__uint_as_float(raw[j][x])) : 0;
           // rotate so that R[t] holds the pair (i0+1, j) of level t+2, i.e. j-1 = t - i0
 #pragma unroll
