@@ -495,8 +495,17 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
             v[k][q2] = (ok && uval[k] && rr < rows) ? src[rr * ld + ucol[k]] : 0.0;
           }
         }
+        // largest exponent field of the unit (1 if only subnormals, 0 if all zero): the largest
+        // high word without its sign bit gives the field; an OR of the magnitudes tells zero
+        uint32_t hmax = 0u, nz = 0u;
 #pragma unroll
-        for (int q2 = 0; q2 < 8; q2++) eu[k] = max(eu[k], exp_field(v[k][q2]));
+        for (int q2 = 0; q2 < 8; q2++) {
+          const uint32_t h = (uint32_t)__double2hiint(v[k][q2]) & 0x7FFFFFFFu;
+          hmax = max(hmax, h);
+          nz |= h | (uint32_t)__double2loint(v[k][q2]);
+        }
+        eu[k] = hmax >> 20;
+        if (eu[k] == 0u && nz != 0u) eu[k] = 1u;
         if (uval[k] && (int)eu[k] > Ereg[k]) exceed = true;
       }
       const bool newp = pp < 0 || period_rows + p.rr > PERIOD || exceed;
@@ -564,7 +573,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
   if (j < P) {
     double sum = 0.0;
     const int b0 = (int)((int64_t)nchunks * j / P), b1 = (int)((int64_t)nchunks * (j + 1) / P);
-    for (int bb = b0; bb < b1; bb++) sum += __ldcg(&p.partials[(size_t)bb * MN + e]);
+#pragma unroll 8
+    for (int bb = b0; bb < b1; bb++) sum += __ldcg(&p.partials[(size_t)bb * MN + e]);  // loads overlap
     red[j * MN + e] = sum;
   }
   __syncthreads();
