@@ -229,6 +229,11 @@ def probe_tsmttsm_items():
                  flops=2 * M * N * K, copies=1)]
 
 
+def probe_tsmttsm1_items():
+    K = 1 << 25
+    return [dict(op="tsmttsm", dt="f64", M=1, N=1, K=K, inplace=False, s=8, bytes=2 * K * 8, flops=2 * K, copies=1)]
+
+
 def probe_split_items():
     return probe_tsmttsm_items()
 
@@ -249,6 +254,7 @@ WORKLOADS = {
                          "split: small case for ncu"),
     "probe-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22 (256 MiB A), alpha 1, beta 0.5: small case for ncu"),
     "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),
+    "probe-tsmttsm1": (probe_tsmttsm1_items, "TSMTTSM FP64 1x1, K = 2^25 (2 x 256 MiB): small case for ncu"),
     "tsmm-sweep": (sweep_items, "TSMM FP64 + complex FP64, alpha 1, beta 0.5, A = 1 GiB per shape, "
                    "M=N in {1..64} + (4,16),(16,4),(8,32), plus in-place FP64 (C = A) for M = N"),
     "tsmttsm-sweep": (tsmttsm_sweep_items, "TSMTTSM FP64 C(MxM) = A^T B, M = N in {1..64}, A and B of 1 GiB "
