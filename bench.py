@@ -313,6 +313,10 @@ def kernel_of(it, method):
             (not wide or Mr * Nr >= 320 * nblk)
         if fp64 and (method == "split" or (method == "auto" and auto_split)):
             return "split_wide_kernel" if wide else "split_tsmttsm_kernel"
+        p2 = lambda x: 1 << (x - 1).bit_length()
+        cap = 16 if it["dt"] == "c64" else 64  # register tiles of the row-streaming kernel
+        if M <= 8 and N <= 8 and p2(M) * p2(N) <= cap:
+            return "tsmttsm_rows_kernel"
         return "tsmttsm_kernel"
     Mr, Nr = (2 * M, 2 * N) if it["dt"] == "c64" else (M, N)
     auto_split = K >= 8192 and Mr * Nr >= 128 and Nr >= 8 and Mr >= 4
@@ -712,8 +716,8 @@ TRAFFIC = {}
 # DRAM traffic of one launch of the dominant kernel family, captured by ncu on a probe shape (the
 # family's launches differ in size, so one per-launch figure of the step does not exist).
 PROBE_TRAFFIC = {
-    "tsmm-sweep": {"kernel": "split_tsmm_kernel<64, 512>", "shape": "FP64 TSMM 64 x 64, K = 2^20, beta 0.5",
-                   "dram_bytes": 1074e6 + 487e6, "algorithmic_bytes": 1611e6},
+    "tsmm-sweep": {"kernel": "split_tsmm_kernel<64>", "shape": "FP64 TSMM 64 x 64, K = 2^20, beta 0.5",
+                   "dram_bytes": 1073.9e6 + 486.3e6, "algorithmic_bytes": 1611e6},
 }
 
 

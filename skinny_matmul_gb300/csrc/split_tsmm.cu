@@ -10,27 +10,29 @@
 //     becomes a 62-bit fixed-point integer and 8 balanced base-256 digits (exact in FP16), as in
 //     the split TSMTTSM (split.cu); A's digits are formed with byte permutes and one HFMA2 per
 //     digit pair (digit_pairs).
-//   * The MMA contraction runs over (digit, column m).  A' (128 rows x 8*MP) holds A's digit planes
-//     with the least significant first: plane p holds digit 8-p.  B' (N x 8*MP) holds B's planes
-//     with the most significant first: plane q holds digit q+1.  For level L = i+j (2..9) the
-//     product of the last (L-1) planes of A' with the first (L-1) planes of B' pairs exactly the
-//     digits with i + j = L, so one MMA chain per level gives D_L(r, n) = sum_{i+j=L} sum_m a_i b_j.
-//   * |D_L| <= 8 * MP * 2^14 <= 2^23: exact in the FP32 TMEM accumulator.
-//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (< 2^80) is formed in integers (level pairs in 32 bits),
-//     its top 61+ bits (from its own leading bit; the rest lies below 2^-61 of |V|) are rounded to
-//     a double with integer instructions and scaled by 2^(e_r + f_n - 2112) in the exponent field;
-//     beta*C is one FMA (the only FP64-pipe operation per output).
-//     Levels >= 10 are dropped (weight below 2^-56 of the leading level).
-//   * Tiles of 128 rows: two threads per row (contraction width 16; four above, with 16 warps per
-//     CTA) read the row's FP64 values straight from global memory into registers; the next
-//     tile's values are loaded right after the current one is sliced, behind the epilogue; the
-//     MMAs of tile t overlap the epilogue of tile t-1 where two TMEM accumulators fit (N <= 32).
-//     Four threads issue the level chains (levels 2+w and 9-w from warp w: 9*MP/16 MMAs each), so
-//     no single warp serialises the whole tile's MMAs.  The epilogue reads the old C values of a
-//     chunk before the TMEM loads of the chunk before it (16-byte pieces where rows are aligned),
-//     so that global and TMEM latencies overlap.
-//   * |D_L| <= 2^22 for contraction widths <= 32 (converted with a float add), <= 2^23 for 64
-//     (converted with integer instructions from the FP32 bit pattern); both exact.
+//   * Digit-stacked MMAs: for A digit i, one tcgen05.mma (M = 128 rows, K = 16 columns m) against
+//     B's digit planes j = 1..9-i stacked along N gives every pair (i, j) with i + j <= 9 at once,
+//     written to the accumulator columns of level L = i + j (level L at columns (L-2) NB of a block
+//     of NB output columns).  Eight MMAs per 16 columns of the contraction form D_L(r, n) =
+//     sum_{i+j=L} sum_m a_i b_j for L = 2..9; levels >= 10 are dropped (weight below 2^-56 of the
+//     leading level).  |D_L| <= 2^14 MP (L - 2) (the top digit is at most 64 in magnitude): exact
+//     in the FP32 TMEM accumulators.
+//   * Epilogue: V = sum_L D_L 2^(8(9-L)) (|V| < 2^74) is formed as a 64-bit integer W = V / 2^12
+//     (level_window), rounded to a double (integer instructions, or the FP64 pipe's conversion
+//     when there is no beta*C) and scaled by 2^(e_r + f_n - 2100) in the exponent field; beta*C
+//     is one FMA.
+//   * Warp roles, hand-offs through mbarriers, no CTA-wide barrier while streaming:
+//       warps 0-7   slicers: two threads per row of a 128-row tile read the row's FP64 values
+//                   (the next tile's are loaded right after a tile is sliced), take the row
+//                   exponent, and write the digit planes into an A' stage; warp 0 then issues
+//                   the tile's MMAs (one elected lane): per block of NB output columns, 8 MP / 16 MMAs into
+//                   one of 2 or 4 TMEM accumulator sets, so that a block's epilogue overlaps the
+//                   next blocks' MMAs;
+//       warps 8-15  epilogue: two warps per TMEM lane quadrant (32 rows), which take alternate
+//                   chunks (8 output columns) of a block; old C values are prefetched chunk by
+//                   chunk (cp.async) into a shared-memory ring several chunks ahead.
+//     Every wait is bounded; a wait that runs out sets the error word and every role stops at its
+//     next wait (C is then incomplete).
 //   * In place with M == N, beta is folded into the diagonal of alpha*B before slicing
 //     (C = A (alpha B + beta I)), so the epilogue neither reads C nor runs the beta FMA.
 // Complex FP64 (interleaved) runs as the real product of doubled width: A (K x 2M), B' (2M x 2N)
@@ -47,12 +49,23 @@ namespace skinny {
 namespace stsmm {
 
 constexpr int ROWS = 128;
-// threads: 256 when two CTAs share an SM (contraction width 16, accumulators of <= 256 columns),
-// otherwise 512 (one CTA of 16 warps per SM); 128 registers either way.  Rows are sliced by up to
-// four threads each (8 columns at least per thread); the epilogue splits the columns over NT/128
-// warp groups -- enough warps to cover its TMEM and global latencies.
 constexpr int DIGITS = 8;
-constexpr int HDR = 8192;      // barriers, TMEM slot, row/column exponents
+constexpr int NSLW = 8;                   // slicer warps 0-7 (two threads per row); warp 0 issues the MMAs
+constexpr int NEPW = 8;                   // epilogue warps 8-15 (two per TMEM lane quadrant)
+constexpr int THREADS = (NSLW + NEPW) * 32;  // 512: four warps per SM sub-partition, 128 registers
+constexpr int MAXAST = 3;                 // A' stages (at most)
+constexpr int CHUNK_BYTES = ROWS * 64;    // one chunk of old C: 8 doubles of each of 128 rows
+constexpr uint32_t SLEEP_MMA = 32;        // ns between polls of the MMA thread
+// Per contraction width MP: the ring of row-exponent records (tiles), the header (barriers, TMEM
+// slot, column exponents, row exponents; a multiple of 1024), and the old-C chunks each epilogue
+// warp group keeps in flight.  At MP = 64 B' (64 KB at N = 64) and one A' stage (128 KB) leave
+// 35 KB: a 3 KB header and two chunks per group fill the 227 KB exactly.
+template <int MP>
+__host__ __device__ constexpr int row_ring() { return MP == 64 ? 4 : 8; }
+template <int MP>
+__host__ __device__ constexpr int hdr_bytes() { return MP == 64 ? 3072 : 5120; }
+template <int MP>
+__host__ __device__ constexpr int c_depth() { return MP == 64 ? 2 : (MP == 32 ? 3 : 4); }
 
 struct Args {
   const double* A;
@@ -60,17 +73,19 @@ struct Args {
   double* C;
   int64_t K, lda, ldb, ldc;  // in doubles (complex: lda, ldc already doubled; ldb in complex elements)
   int M, N;                  // real widths (complex: 2M, 2N)
-  int NM;                    // MMA N: 16, 32 or 64
+  int NM;                    // output width padded: 16, 32 or 64
+  int NB, ncb;               // output columns per accumulator block (16 or 32), blocks per tile
+  int nsets;                 // TMEM accumulator sets (512 / (8 NB))
+  int nast;                  // A' stages
+  uint32_t astage;           // bytes of one A' stage (8 planes x 128 rows x MP x FP16)
+  uint32_t bbytes;           // bytes reserved for B' (8 planes x NM x MP x FP16, 1024-aligned)
   int cplx;                  // B is complex (alpha, beta complex)
   double alpha[2], beta[2];
   int beta_zero, inplace, vec;  // vec: rows of A may be read as 16-byte pairs
   int fold;                     // beta folded into B's diagonal (in place, M == N); beta_zero then set
   int vecc;                     // rows of C may be read and written as 16-byte pairs
   int64_t ntiles;
-  uint32_t abuf;  // bytes of one A' buffer
-  int nabuf;      // A' buffers (1 or 2)
-  int ntbuf;      // TMEM accumulator buffers (1 or 2)
-  int tmem_cols;
+  int la;  // MMA issue: 0 by slicer warp 0, else by epilogue warp 8 this many tiles ahead
   int* err;
 };
 
@@ -81,15 +96,18 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo) {
   d |= (uint64_t)1 << 46;
   return d;
 }
+// issued by one elected lane of a converged warp, so that the operands stay warp-uniform
 __device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "{\n .reg .pred p, e;\n elect.sync _|e, 0xffffffff;\n setp.ne.b32 p, %4, 0;\n"
+      " @e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
       "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
+  asm volatile(
+      "{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n"
+      " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(smem_u32(bar))
+      : "memory");
 }
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -166,342 +184,410 @@ __device__ __forceinline__ void load_row(const Args& p, int64_t r0, int row, int
   }
 }
 
-// x * 2^E for a signed 64-bit integer x, rounded to 53 bits (ties away from zero); |x| < 2^63,
-// 0 for x == 0.  Branch-free: for x == 0 the normalising shift is masked to 0 and the final select
-// returns 0.
-__device__ __forceinline__ double i64_to_double(long long x, int E) {
-  const unsigned long long sgn = (unsigned long long)x & 0x8000000000000000ull;
-  unsigned long long m = (unsigned long long)(x < 0 ? -x : x);
-  const int z = __clzll((long long)m);  // >= 1 for x != 0
-  m <<= (z & 63);                       // leading one at bit 63
-  unsigned long long mant = (m + 0x400ull) >> 11;  // round on bit 10; may carry to 2^53
-  int ex = 63 - z + E;
-  const unsigned long long carry = mant >> 53;
-  mant >>= carry;
-  ex += (int)carry;
-  const double r =
-      __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-  return x ? r : 0.0;
+// Level sums to integers on the FMA pipe.  An FP32 accumulator holds an exact integer D; for
+// |D| <= 2^22, D + 1.5 * 2^23 lies in [2^23, 2^24], where FP32 spacing is 1, so the sum's bit
+// pattern is 0x4B400000 + D.  For |D| < 2^24 the same with 1.5 * 2^25 (spacing 4) gives D's
+// multiple of 4, h, and D - h (|D - h| <= 2) follows exactly; with 1.5 * 2^24 (spacing 2) the
+// pattern 0x4BC00000 + D / 2 gives D to within 1.  (A float-to-int conversion instruction runs on
+// GB300's narrow FP64 pipe, and integer bit manipulation on the ALU pipe, which the rest of the
+// epilogue keeps busy.)
+__device__ __forceinline__ int f32_int22(float f) { return __float_as_int(f + 12582912.0f) - 0x4B400000; }
+__device__ __forceinline__ int f32_int24(float f) {
+  const float t = f + 50331648.0f;  // 1.5 * 2^25
+  const float h = t - 50331648.0f;  // exact: D's nearest multiple of 4
+  return 4 * (__float_as_int(t) - 0x4C400000) + f32_int22(f - h);
 }
+__device__ __forceinline__ int f32_int23_near(float f) { return 2 * (__float_as_int(f + 25165824.0f) - 0x4BC00000); }
 
-// The integer value of an FP32 holding an exact integer with |f| < 2^24, with integer instructions
-// only (a float-to-int conversion instruction shares GB300's narrow FP64 pipe, the unit the beta
-// FMA already needs): the mantissa with its implicit bit, shifted right by 150 - exponent (a
-// funnel shift that clamps at 32, so 0.0 gives 0), then the sign.
-__device__ __forceinline__ int f32_int_exact(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t mag = __funnelshift_rc((u & 0x7FFFFFu) | 0x800000u, 0u, 150u - ((u >> 23) & 0xFFu));
-  const int s = (int)u >> 31;  // 0 or -1
-  return ((int)mag ^ s) - s;
-}
-
-// The double of column x of a chunk: V = sum_L D_L 2^(8(9-L)) from the eight FP32 level sums in
-// raw[L][x] (exact integers), times 2^E.
+// The product of a row and a column from the eight FP32 level sums in raw[L][x] (exact integers
+// D_2..D_9 of V = sum_L D_L 2^(8(9-L))) is V * 2^(er + fc - 2112) for row and column exponent
+// fields er and fc.  level_window forms W = V / 2^12 as a 64-bit integer:
+//   * Sizes: the top digit is at most 64 in magnitude, the others 128, so |D_2| <= 2^12 MP and
+//     |D_L| <= 2^14 MP (L - 2) for L >= 3.  At MP <= 32 every level is within 2^22; at MP = 64
+//     levels 2..6 are, level 7 (< 2^23) is converted exactly in two steps, and levels 8 and 9
+//     (weights 2^8 and 1 in V) to within 1, which the 2^12 that W drops below covers.
+//   * Pairs P = D_L * 256 + D_{L+1} fit 32 bits (|P| < 2^31 for every pair), and |V| < 2^74 (V is
+//     the exact sum of MP products of 62-bit fixed-point values, shifted down by 2^56), so
+//     W = P1 2^36 + P2 2^20 + P3 2^4 + floor(P4 / 2^12) is a 64-bit integer (|W| < 2^62) within
+//     one unit of V / 2^12.  Dropping those 12 bits keeps W relative to the largest possible V at
+//     2^-62, below the fixed-point truncation of the inputs themselves.
+// The double W * 2^(er + fc - 2100) then comes from one of two finishers (same accuracy): the
+// integer one runs on the ALU pipe, the conversion one on the FP64 pipe, which is free for it
+// when the epilogue has no beta FMA.  W == 0 and results below the normal range give 0.
 template <int MP>
-__device__ __forceinline__ double level_value(const uint32_t (&raw)[8][8], int x, int E) {
-  int dl[8];
+__device__ __forceinline__ long long level_window(const uint32_t (&raw)[8][8], int x) {
+  int d[8];
 #pragma unroll
   for (int L = 0; L < 8; L++) {
     const float f = __uint_as_float(raw[L][x]);
-    // |D_L| <= (L-1) * MP * 2^14: up to 2^22 the magic add is exact (levels 2..5 at MP = 64)
-    dl[L] = (MP <= 32 || L < 4) ? __float_as_int(f + 12582912.0f) - 0x4B400000 : f32_int_exact(f);
+    d[L] = (MP <= 32 || L < 5) ? f32_int22(f) : (L == 5 ? f32_int24(f) : f32_int23_near(f));
   }
-  // level pairs in 32 bits: |D_L * 256 + D_{L+1}| < 2^31 for every pair (the largest, D_8 * 256 +
-  // D_9 at MP = 64, is below 1.9e9)
-  const int P1 = dl[0] * 256 + dl[1], P2 = dl[2] * 256 + dl[3];
-  const int P3 = dl[4] * 256 + dl[5], P4 = dl[6] * 256 + dl[7];
-  // H = levels 2..5, Lo = levels 6..9 (each |.| < 2^48), V = H * 2^32 + Lo < 2^80.
-  const long long H = ((long long)P1 << 16) + P2;
-  const long long Lo = ((long long)P3 << 16) + P4;
-  // the top bits of V from its own leading bit: shift H up by k = clz(|H|) - 2, so that
-  // |H << k| < 2^62 and adding the |Lo| part (< 2^48) cannot pass 2^63 (k = 32, also for H = 0:
-  // V fits in 64 bits and is kept whole); at least 61 bits are kept, the bits of Lo dropped lie
-  // below 2^-61 of |V|.  They are rounded to a double with integer instructions (a conversion
-  // instruction from 64-bit integers runs on the FP64 pipe, the scarce unit here)
-  const long long aH = H < 0 ? -H : H;
-  const int k = min(32, __clzll(aH) - 2);
-  const long long top = (H << k) + (Lo >> (32 - k));
-  return i64_to_double(top, E - k);
+  const int P1 = d[0] * 256 + d[1], P2 = d[2] * 256 + d[3];
+  const int P3 = d[4] * 256 + d[5], P4 = d[6] * 256 + d[7];
+  return ((long long)P1 << 36) + (long long)P2 * (1 << 20) + (long long)P3 * 16 + (long long)(P4 >> 12);
+}
+// Integer finisher, ex = er + fc - 1014 (the biased exponent field of the result when W has its
+// leading one at bit 63): normalise |W| so that its leading one is bit 63, round on bit 10 (ties
+// away from zero), and add the exponent field below the leading one, so that a mantissa carry
+// raises the exponent.
+__device__ __forceinline__ double window_int(long long W, int ex) {
+  const uint32_t sgn = (uint32_t)((unsigned long long)W >> 32) & 0x80000000u;
+  const unsigned long long m = (unsigned long long)(W < 0 ? -W : W);
+  const int z = __clzll((long long)m);                       // 64 for W == 0
+  const unsigned long long n = m << (z & 63);                 // leading one at bit 63 (0 for W == 0)
+  const unsigned long long r = (n >> 11) + ((n >> 10) & 1);  // 53 bits, or 2^53 after a carry
+  const int ef = ex - z;                                      // biased exponent field of the result
+  const uint32_t hi = ((uint32_t)(ef - 1) << 20) + (uint32_t)(r >> 32);
+  const bool ok = n != 0 && ef > 0;
+  return __hiloint2double(ok ? (int)(hi | sgn) : 0, ok ? (int)(uint32_t)r : 0);
+}
+// Conversion finisher, es = er + fc - 2100: the FP64 pipe's int64 -> double conversion (rounded
+// to nearest; exact scaling follows), then es added to the exponent field.
+__device__ __forceinline__ double window_cvt(long long W, int es) {
+  const double d = __ll2double_rn(W);
+  const int hi = __double2hiint(d), lo = __double2loint(d);
+  const int e0 = (hi >> 20) & 0x7FF;  // 0 only for W == 0
+  const bool ok = e0 != 0 && e0 + es > 0;
+  return __hiloint2double(ok ? (int)((uint32_t)hi + ((uint32_t)es << 20)) : 0, ok ? lo : 0);
 }
 
-// contraction width 16 (TMEM <= 256 columns, shared memory < 114 KB): two CTAs per SM, so that one
-// CTA's barriers overlap the other's work
-template <int MP, int NT>
-__global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) split_tsmm_kernel(const Args p) {
-  constexpr int TPR = NT / ROWS;                         // column parts of the epilogue
-  constexpr int TPS = MP / 8 < TPR ? MP / 8 : TPR;       // threads slicing a row
-  constexpr int PART = MP / TPS;                         // columns sliced per thread
-  extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bar_mma = reinterpret_cast<uint64_t*>(smem + 32);   // [2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 64);
-  int* erow = reinterpret_cast<int*>(smem + 128);               // [2 parity][TPR parts][ROWS]
-  int* fcol = reinterpret_cast<int*>(smem + 128 + 2 * TPR * ROWS * 4);  // [64]
-  const int M = p.M, N = p.N, NM = p.NM;
-  const uint32_t lbo_a = ROWS * 16, lbo_b = (uint32_t)NM * 16;
-  unsigned char* bdig = smem + HDR;                               // B' (NM x 8*MP), 1024-aligned
-  const uint32_t bdig_bytes = (uint32_t)(8 * MP / 8) * lbo_b;
-  unsigned char* adig = bdig + ((bdig_bytes + 1023) & ~1023u);   // A' buffers
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// bounded wait that also gives up as soon as another thread of the CTA has given up; sleep_ns
+// between polls for the MMA thread, which waits most of the time
+__device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile int* ab, int* err,
+                                        uint32_t sleep_ns = 0) {
+  for (uint32_t i = 0; i < kWaitPolls; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*ab) return false;
+    if (sleep_ns) __nanosleep(sleep_ns);
+  }
+  *ab = 1;
+  if (err) atomicExch(err, SKINNY_DEVERR_TIMEOUT);
+  return false;
+}
+// asynchronous global -> shared copies of old C (src_bytes < size zero-fills the rest; 0 reads nothing)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
+template <int MP>
+__global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
+  constexpr int PART = MP / 2;         // A values per slicer thread (two threads per row)
+  constexpr int CD = c_depth<MP>();    // old-C chunks in flight per epilogue thread
+  constexpr int RE = row_ring<MP>(), HDR = hdr_bytes<MP>();
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* afull = reinterpret_cast<uint64_t*>(smem);          // [MAXAST] A' stage written
+  uint64_t* aempty = reinterpret_cast<uint64_t*>(smem + 32);    // [MAXAST] its MMAs completed
+  uint64_t* tfull = reinterpret_cast<uint64_t*>(smem + 64);     // [4] accumulator set complete
+  uint64_t* tempty = reinterpret_cast<uint64_t*>(smem + 96);    // [4] accumulator set read
+  uint64_t* efull = reinterpret_cast<uint64_t*>(smem + 128);    // [RE] row exponents written
+  uint64_t* eempty = reinterpret_cast<uint64_t*>(smem + 192);   // [RE] row exponents read
+  uint64_t* mfin = reinterpret_cast<uint64_t*>(smem + 256);     // every MMA of the CTA completed
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + 264);
+  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + 268);
+  int* fcol = reinterpret_cast<int*>(smem + 512);               // [64] column exponents
+  int* erow = reinterpret_cast<int*>(smem + 1024);              // [RE][ROWS] row exponents
+  unsigned char* bdig = smem + HDR;                             // B' (1024-aligned)
+  unsigned char* adig = bdig + p.bbytes;                        // A' stages
+  unsigned char* cbuf = adig + (size_t)p.nast * p.astage;       // [2 groups][CD][ROWS][8 doubles] old C
+  const int M = p.M, N = p.N, NB = p.NB;
+  // B' per block of NB output columns: rows j * NB + n (digit j + 1 of column n), K-major over
+  // m in octets of 8 rows x 16 bytes (no swizzle); bytes between k-octets and between blocks:
+  const uint32_t bko = 128u * (uint32_t)NB, bcb = (uint32_t)(MP / 8) * bko;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t t_begin = p.ntiles * blockIdx.x / gridDim.x;
   const int64_t t_end = p.ntiles * (blockIdx.x + 1) / gridDim.x;
   const int nt = (int)(t_end - t_begin);
 
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"(p.tmem_cols));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) {  // four issuing threads commit to each tile's barrier
-    mbar_init(&bar_mma[0], 4);
-    mbar_init(&bar_mma[1], 4);
+  if (tid == 0) {
+    for (int s = 0; s < MAXAST; s++) {
+      mbar_init(&afull[s], NSLW);
+      mbar_init(&aempty[s], 1);
+    }
+    for (int k = 0; k < 4; k++) {
+      mbar_init(&tfull[k], 1);
+      mbar_init(&tempty[k], NEPW);
+    }
+    for (int e = 0; e < RE; e++) {
+      mbar_init(&efull[e], NSLW);
+      mbar_init(&eempty[e], NEPW);
+    }
+    mbar_init(mfin, 1);
+    *abort_f = 0;
     fence_mbar_init();
   }
   // ---- B' = digits of alpha * B: column exponents, then (n, m-octet) units -------------------
-  if (tid < NM) {
+  if (tid < p.NM) {
     uint32_t f = 0;
     for (int m = 0; m < M; m++) f = max(f, exp_field(alpha_b(p, m, tid)));
     fcol[tid] = (int)f;
   }
   __syncthreads();
-  for (int u = tid; u < NM * (MP / 8); u += NT) {
-    const int n = u % NM, mo = u / NM;
+  for (int u = tid; u < p.NM * (MP / 8); u += THREADS) {
+    const int n = u % p.NM, mo = u / p.NM;
     float d[8][DIGITS];
     bool ng[8];
 #pragma unroll
     for (int q2 = 0; q2 < 8; q2++) digits_of(alpha_b(p, mo * 8 + q2, n), (uint32_t)fcol[n], d[q2], ng[q2]);
+    unsigned char* bcol = bdig + (uint32_t)(n / NB) * bcb;
 #pragma unroll
     for (int j = 0; j < DIGITS; j++) {
       uint4 w = make_uint4(pack2(d[0][j], d[1][j], ng[0], ng[1]), pack2(d[2][j], d[3][j], ng[2], ng[3]),
                            pack2(d[4][j], d[5][j], ng[4], ng[5]), pack2(d[6][j], d[7][j], ng[6], ng[7]));
-      *reinterpret_cast<uint4*>(bdig + kmaj(n, (j * MP + mo * 8) / 8, lbo_b)) = w;
+      *reinterpret_cast<uint4*>(bcol + kmaj(j * NB + n % NB, mo, bko)) = w;
     }
   }
+  fence_proxy_async_smem();
   tc_before();
   __syncthreads();
   tc_after();
   const uint32_t tmem = *tslot;
 
-  // kind::f16 with FP16 A and B (a/b format 0), FP32 accumulators, N = NM, M = 128
-  const uint32_t idesc = (1u << 4) | ((uint32_t)(NM >> 3) << 17) | ((128u >> 4) << 24);
-  const int row = tid & (ROWS - 1), part = tid >> 7;
-  const bool slicer = part < TPS;
-  const int m0 = (slicer ? part : 0) * PART;
-  int uses[2] = {0, 0};
-  bool bail = false;
-
-  auto epilogue = [&](int it) {
-    const int64_t t = t_begin + it;
-    const int64_t r0 = t * ROWS;
-    const int rows = (int)((p.K - r0) < ROWS ? (p.K - r0) : ROWS);
-    const int q = warp & 3;
-    const int r = 32 * q + lane;
-    const int* er = erow + ((it & 1) * TPR) * ROWS;
-    const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((it % p.ntbuf) * 8 * NM);
-    // TPR column parts of even width (complex (re, im) pairs stay together), one per warp group
-    const int pw = ((N + TPR - 1) / TPR + 1) & ~1;
-    const int n0 = min(N, (warp >> 2) * pw), n1 = min(N, n0 + pw);
-    const bool live = r < rows;
-    double* crow = p.C + (r0 + r) * p.ldc;
-    // a chunk of 8 columns inside [n0, n1) is moved as four 16-byte pieces when C's rows allow it
-    auto whole = [&](int c0) { return p.vecc && c0 >= n0 && c0 + 8 <= n1; };
-    // old C values of a chunk (in place: this row of A, not yet overwritten); issued before the
-    // TMEM loads of the chunk before it, so that the global and TMEM latencies overlap
-    auto load_c = [&](int c0, double (&cv)[8]) {
-      if (p.beta_zero || !live) {
-#pragma unroll
-        for (int x = 0; x < 8; x++) cv[x] = 0.0;
-      } else if (whole(c0)) {
-#pragma unroll
-        for (int x = 0; x < 8; x += 2) {
-          const double2 w = *reinterpret_cast<const double2*>(crow + c0 + x);
-          cv[x] = w.x;
-          cv[x + 1] = w.y;
-        }
-      } else {
-#pragma unroll
-        for (int x = 0; x < 8; x++) {
-          const int n = c0 + x;
-          cv[x] = (n >= n0 && n < n1) ? crow[n] : 0.0;
-        }
+  // MMA issue by one warp, converged, one elected lane: per block of NB output columns, digit
+  // i + 1 of A against B planes 0 .. 7 - i (kind::f16, FP16 A and B, FP32 accumulators,
+  // M = 128, N = (8 - i) NB) into the next accumulator set.  The issuing warp is slicer warp 0
+  // (after it has sliced its rows of the tile) or, where the epilogue has slack (no beta FMA, no
+  // old C, few MMAs per tile) and the accumulator sets allow p.la >= 1 tiles of lookahead,
+  // epilogue warp 8 (tile t + la before it drains tile t).
+  int mjob = 0;
+  auto issue_tile = [&](int it) -> bool {
+    const int s = it % p.nast;
+    if (!wait_ab(&afull[s], (uint32_t)((it / p.nast) & 1), abort_f, p.err, SLEEP_MMA)) return false;
+    tc_after();
+    const uint32_t as = smem_u32(adig) + (uint32_t)s * p.astage;
+    for (int cb = 0; cb < p.ncb; cb++, mjob++) {
+      const int k = mjob % p.nsets;
+      if (mjob >= p.nsets) {
+        if (!wait_ab(&tempty[k], (uint32_t)((mjob / p.nsets - 1) & 1), abort_f, p.err, SLEEP_MMA)) return false;
+        tc_after();
       }
-    };
-    // 128 registers: no room for a second chunk of C, so a chunk's own C loads go out just
-    // before its TMEM loads
-    constexpr bool AHEAD = false;
-    double cold[8], cnext[8];
-    if (AHEAD && n0 < n1) load_c(n0 & ~7, cold);
-    for (int c0 = (n0 & ~7); c0 < n1; c0 += 8) {
-      if (!AHEAD) load_c(c0, cold);
-      uint32_t raw[8][8];
+      const uint32_t dcol = tmem + (uint32_t)(k * 8 * NB);
+      const uint32_t bb = smem_u32(bdig) + (uint32_t)cb * bcb;
 #pragma unroll
-      for (int L = 0; L < 8; L++) tmem_ld8(tbase + (uint32_t)(L * NM + c0), raw[L]);
-      if (AHEAD && c0 + 8 < n1) load_c(c0 + 8, cnext);
-      tmem_wait();
-      if (live) {
-        // all eight columns are formed (columns beyond N hold zero digits and exponent 0) and
-        // masked only at the store; beta * C with the dtype test outside the column loop
-        const int e = er[r] - 2112 + 32;
-        double out[8];
+      for (int ks = 0; ks < MP / 16; ks++)
 #pragma unroll
-        for (int x = 0; x < 8; x++) out[x] = level_value<MP>(raw, x, e + fcol[c0 + x]);
-        if (!p.beta_zero) {
-          if (!p.cplx) {
-#pragma unroll
-            for (int x = 0; x < 8; x++) out[x] = fma(p.beta[0], cold[x], out[x]);
-          } else {
-#pragma unroll
-            for (int x = 0; x < 8; x += 2) {  // (re, im) pairs: c0 is a multiple of 8
-              const double cr = cold[x], ci = cold[x + 1];
-              out[x] = fma(p.beta[0], cr, fma(-p.beta[1], ci, out[x]));
-              out[x + 1] = fma(p.beta[0], ci, fma(p.beta[1], cr, out[x + 1]));
-            }
-          }
-        }
-        if (whole(c0)) {
-#pragma unroll
-          for (int x = 0; x < 8; x += 2) *reinterpret_cast<double2*>(crow + c0 + x) = make_double2(out[x], out[x + 1]);
-        } else {
-#pragma unroll
-          for (int x = 0; x < 8; x++) {
-            const int n = c0 + x;
-            if (n >= n0 && n < n1) crow[n] = out[x];
-          }
-        }
-      }
-      if (AHEAD) {
-#pragma unroll
-        for (int x = 0; x < 8; x++) cold[x] = cnext[x];
-      }
+        for (int i = 0; i < DIGITS; i++)
+          mma_f16(dcol + (uint32_t)(i * NB), make_desc(as + (uint32_t)(i * MP * 256 + ks * 4096), 2048u),
+                  make_desc(bb + (uint32_t)(2 * ks) * bko, bko),
+                  (1u << 4) | ((uint32_t)(((DIGITS - i) * NB) >> 3) << 17) | ((128u >> 4) << 24),
+                  (ks | i) ? 1u : 0u);
+      mma_commit(&tfull[k]);
     }
+    mma_commit(&aempty[s]);
+    return true;
   };
-  auto wait_mma = [&](int tile_it) -> bool {  // wait until the MMAs of local tile tile_it completed
-    const int b = tile_it & 1;
-    return mbar_wait_bounded(&bar_mma[b], (uint32_t)((uses[b] - 1) & 1), p.err);
-  };
-
-  // A values of the tile being sliced; the next tile's are loaded into the same registers right
-  // after slicing (the old values are dead then), so their latency hides behind the epilogue
-  double v[PART];
-  auto load_tile = [&](int it) {
-    const int64_t r1 = (t_begin + it) * ROWS;
-    load_row<PART>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, v);
-  };
-  if (nt > 0 && slicer) load_tile(0);
-  for (int it = 0; it < nt && !bail; it++) {
-    // row exponents: each part of the columns, combined through shared memory
-    int* er = erow + ((it & 1) * TPR) * ROWS;
-    if (slicer) {
+  if (warp < NSLW) {
+    // ---- slicers: row = tid / 2, columns [m0, m0 + PART) ------------------------------------
+    const int row = tid >> 1, part = tid & 1, m0 = part * PART;
+    double v[PART];
+    auto load_tile = [&](int it) {
+      const int64_t r1 = (t_begin + it) * ROWS;
+      load_row<PART>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, v);
+    };
+    if (nt > 0) load_tile(0);
+    for (int it = 0; it < nt; it++) {
+      const int s = it % p.nast, es = it % RE;
       uint32_t emax = 0;
 #pragma unroll
       for (int j = 0; j < PART; j++) emax = max(emax, exp_field(v[j]));
-      er[part * ROWS + row] = (int)emax;
-    }
-    __syncthreads();
-    int e_row = er[row];
+      emax = max(emax, (uint32_t)__shfl_xor_sync(0xffffffffu, emax, 1));
+      bool ok = *abort_f == 0;
+      if (ok && it >= RE) ok = wait_ab(&eempty[es], (uint32_t)((it / RE - 1) & 1), abort_f, p.err);
+      if (ok && it >= p.nast) ok = wait_ab(&aempty[s], (uint32_t)((it / p.nast - 1) & 1), abort_f, p.err);
+      if (!__all_sync(0xffffffffu, ok)) break;  // the whole warp leaves together
+      if (part == 0) erow[es * ROWS + row] = (int)emax;
+      unsigned char* A_ = adig + (size_t)s * p.astage;
 #pragma unroll
-    for (int q2 = 1; q2 < TPS; q2++) e_row = max(e_row, er[q2 * ROWS + row]);
-    // the A' buffer is free once the MMAs that read it completed
-    if ((p.nabuf == 1 && it > 0) || (p.nabuf == 2 && it > 1)) {
-      bool ok = wait_mma(it - p.nabuf);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
-        break;
-      }
-    }
-    unsigned char* A_ = adig + (size_t)(it % p.nabuf) * p.abuf;
+      for (int o = 0; o < PART / 8; o++) {
+        const int mo = (m0 >> 3) + o;
+        if (mo * 8 >= M) {  // zero padding columns: zero digits
 #pragma unroll
-    for (int o = 0; o < (slicer ? PART / 8 : 0); o++) {
-      const int mo = (m0 >> 3) + o;
-      if (mo * 8 >= M) {  // zero padding columns: zero digits
+          for (int pl = 0; pl < DIGITS; pl++)
+            *reinterpret_cast<uint4*>(A_ + (uint32_t)(pl * MP * 256) + kmaj(row, mo, 2048u)) = make_uint4(0, 0, 0, 0);
+          continue;
+        }
+        uint32_t dp[4][DIGITS];  // element pairs (0,1), (2,3), (4,5), (6,7) of the octet
+#pragma unroll
+        for (int q2 = 0; q2 < 4; q2++) {
+          uint32_t gha, gla, ghb, glb;
+          bool na, nb;
+          g_words(v[o * 8 + 2 * q2], emax, gha, gla, na);
+          g_words(v[o * 8 + 2 * q2 + 1], emax, ghb, glb, nb);
+          digit_pairs(gha, gla, na, ghb, glb, nb, dp[q2]);
+        }
+        // plane pl holds digit pl + 1: 128 rows x MP columns, k-octets 2048 bytes apart
 #pragma unroll
         for (int pl = 0; pl < DIGITS; pl++)
-          *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) = make_uint4(0, 0, 0, 0);
-        continue;
+          *reinterpret_cast<uint4*>(A_ + (uint32_t)(pl * MP * 256) + kmaj(row, mo, 2048u)) =
+              make_uint4(dp[0][pl], dp[1][pl], dp[2][pl], dp[3][pl]);
       }
-      uint32_t dp[4][DIGITS];  // element pairs (0,1), (2,3), (4,5), (6,7) of the octet
-#pragma unroll
-      for (int q2 = 0; q2 < 4; q2++) {
-        uint32_t gha, gla, ghb, glb;
-        bool na, nb;
-        g_words(v[o * 8 + 2 * q2], (uint32_t)e_row, gha, gla, na);
-        g_words(v[o * 8 + 2 * q2 + 1], (uint32_t)e_row, ghb, glb, nb);
-        digit_pairs(gha, gla, na, ghb, glb, nb, dp[q2]);
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&efull[es]);
+        mbar_arrive(&afull[s]);
       }
-#pragma unroll
-      for (int pl = 0; pl < DIGITS; pl++) {
-        const int i = 7 - pl;  // 0-based digit index held by plane pl
-        *reinterpret_cast<uint4*>(A_ + kmaj(row, (pl * MP + mo * 8) / 8, lbo_a)) =
-            make_uint4(dp[0][i], dp[1][i], dp[2][i], dp[3][i]);
-      }
+      if (it + 1 < nt) load_tile(it + 1);  // in flight while this tile's MMAs run
+      // a wait that runs out sets the abort flag, which the slicers see at the next tile
+      if (warp == 0 && p.la == 0) issue_tile(it);
     }
-    if (tid < ROWS) er[tid] = e_row;  // the epilogue of this tile reads er[r]
-    fence_proxy_async_smem();
-    // one accumulator: the epilogue of tile it-1 needs no barrier after this tile's slicing (it
-    // reads TMEM and C, not A'), so warps go from slicing straight into it; the barrier that
-    // ends the epilogue also completes A' for the MMAs
-    const bool drain_first = p.ntbuf == 1 && it > 0;
-    if (!drain_first) {
-      tc_before();
-      __syncthreads();
+    if (warp == 0 && p.la == 0) {
+      mma_commit(mfin);  // completes once every MMA issued by the elected lanes has
+      mbar_wait_bounded(mfin, 0, nullptr);
     }
-    if (it + 1 < nt && slicer) load_tile(it + 1);  // in flight during the epilogue and the MMAs
-    if (drain_first) {  // one accumulator: drain tile it-1 before tile it's MMAs
-      if (p.nabuf != 1) {
-        bool ok = wait_mma(it - 1);
-        if (__syncthreads_or(!ok)) {
-          bail = true;
-          break;
+    __syncwarp();
+  } else {
+    // ---- epilogue: warps 8 + q and 12 + q read TMEM lanes 32q..32q+31 (rows of the tile) ------
+    const int q = warp & 3, r = 32 * q + lane, eg = (warp - NSLW) >> 2;
+    const int CH = (N + 7) >> 3;        // chunks of 8 output columns per row
+    const int CHg = (CH - eg + 1) >> 1;  // chunks c = eg, eg + 2, .. of this warp per tile
+    const int cpb = NB >> 3;            // chunks per block (even)
+    const bool need_c = !p.beta_zero;
+    // the FP64-pipe finisher where the epilogue runs no beta FMA on that pipe (measured: with the
+    // FMA, the conversion makes the FP64 pipe the bottleneck even on one warp group)
+    const bool cvt = !need_c;
+    const int64_t gtot = (int64_t)nt * CHg;
+    // old C of this warp's chunk g (tile g / CHg, chunk eg + 2 (g % CHg)) into ring slot g % CD
+    auto issue = [&](int64_t g) {
+      if (g < gtot) {
+        const int it = (int)(g / CHg), c = eg + 2 * (int)(g % CHg);
+        const int64_t rr = (t_begin + it) * ROWS + r;
+        const bool live = rr < p.K;
+        const double* src = p.C + rr * p.ldc + 8 * c;
+        unsigned char* dst = cbuf + (size_t)(eg * CD + (int)(g % CD)) * CHUNK_BYTES + r * 64;
+        if (p.vecc) {
+#pragma unroll
+          for (int x = 0; x < 4; x++) {
+            const int left = N - (8 * c + 2 * x);
+            const uint32_t bytes = live ? (uint32_t)(left >= 2 ? 16 : (left == 1 ? 8 : 0)) : 0u;
+            cp_async16(dst + 16 * x, bytes ? (const void*)(src + 2 * x) : (const void*)p.C, bytes);
+          }
+        } else {
+#pragma unroll
+          for (int x = 0; x < 8; x++) {
+            const uint32_t bytes = (live && 8 * c + x < N) ? 8u : 0u;
+            cp_async8(dst + 8 * x, bytes ? (const void*)(src + x) : (const void*)p.C, bytes);
+          }
         }
       }
-      tc_after();
-      epilogue(it - 1);
-      tc_before();
-      __syncthreads();
-    }
-    if (lane == 0 && warp < 4) {  // warp w issues the chains of levels 2 + w and 9 - w (9 K-steps of MP/16)
-      tc_after();
-      const uint32_t a0 = smem_u32(A_), b0 = smem_u32(bdig);
-      const uint32_t dcol = tmem + (uint32_t)((it % p.ntbuf) * 8 * NM);
-#pragma unroll
-      for (int side = 0; side < 2; side++) {
-        const int L = side ? 9 - warp : 2 + warp;
-        const int kq = (L - 1) * MP / 16;  // K-steps of 16
-        const int ka = (9 - L) * MP / 8;   // first k-octet of A' for this level
-        for (int ks = 0; ks < kq; ks++)
-          mma_f16(dcol + (uint32_t)((L - 2) * NM), make_desc(a0 + (uint32_t)(ka + 2 * ks) * lbo_a, lbo_a),
-                   make_desc(b0 + (uint32_t)(2 * ks) * lbo_b, lbo_b), idesc, ks > 0 ? 1u : 0u);
-      }
-      mma_commit(&bar_mma[it & 1]);  // one of the four arrivals that complete the tile's phase
-    }
-    uses[it & 1]++;
-    if (p.ntbuf == 2 && it > 0) {  // the previous tile's epilogue overlaps this tile's MMAs
-      bool ok = wait_mma(it - 1);
-      if (__syncthreads_or(!ok)) {
-        bail = true;
+      cp_async_commit();
+    };
+    if (need_c)
+      for (int g = 0; g < CD - 1; g++) issue(g);
+    const bool issuer = p.la > 0 && warp == NSLW;
+    if (issuer)
+      for (int j = 0; j < p.la && j < nt; j++) issue_tile(j);
+    int64_t g = 0;
+    int job = 0;
+    bool ok = true;
+    for (int it = 0; it < nt && ok; it++) {
+      const int es = it % RE;
+      if (issuer && it + p.la < nt) issue_tile(it + p.la);  // a timeout sets the abort flag
+      const int64_t rr = (t_begin + it) * ROWS + r;
+      const bool live = rr < p.K;
+      ok = wait_ab(&efull[es], (uint32_t)((it / RE) & 1), abort_f, p.err);
+      if (!__all_sync(0xffffffffu, ok)) {
+        ok = false;
         break;
       }
-      tc_after();
-      epilogue(it - 1);
-      tc_before();
-      __syncthreads();
+      const int e = erow[es * ROWS + r] - 1014;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&eempty[es]);
+      double* crow = p.C + rr * p.ldc;
+      for (int cb = 0; cb < p.ncb; cb++, job++) {
+        const int k = job % p.nsets;
+        ok = wait_ab(&tfull[k], (uint32_t)((job / p.nsets) & 1), abort_f, p.err);
+        if (!__all_sync(0xffffffffu, ok)) {
+          ok = false;
+          break;
+        }
+        tc_after();
+        const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(k * 8 * NB);
+        const int c_hi = min(CH, (cb + 1) * cpb);
+        for (int c = cb * cpb + eg; c < c_hi; c += 2, g++) {
+          if (need_c) issue(g + CD - 1);  // into the slot of chunk g - 1, read in full already
+          uint32_t raw[8][8];
+#pragma unroll
+          for (int L = 0; L < 8; L++) tmem_ld8(tb + (uint32_t)(L * NB + 8 * (c - cb * cpb)), raw[L]);
+          double cold[8];
+          if (need_c) {
+            cp_async_wait<CD - 1>();  // this thread's copies of chunk g have landed
+            const double2* cs =
+                reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + (int)(g % CD)) * CHUNK_BYTES + r * 64);
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+              const double2 w = cs[x];
+              cold[2 * x] = w.x;
+              cold[2 * x + 1] = w.y;
+            }
+          }
+          tmem_wait();
+          if (live) {
+            // all eight columns are formed (columns beyond N hold zero digits and exponent 0) and
+            // masked only at the store
+            const int c0 = 8 * c;
+            double out[8];
+            if (cvt) {
+#pragma unroll
+              for (int x = 0; x < 8; x++) out[x] = window_cvt(level_window<MP>(raw, x), e + fcol[c0 + x] - 1086);
+            } else {
+#pragma unroll
+              for (int x = 0; x < 8; x++) out[x] = window_int(level_window<MP>(raw, x), e + fcol[c0 + x]);
+            }
+            if (need_c) {
+              if (!p.cplx || p.beta[1] == 0.0) {  // a real beta scales both parts of a complex C alike
+#pragma unroll
+                for (int x = 0; x < 8; x++) out[x] = fma(p.beta[0], cold[x], out[x]);
+              } else {
+#pragma unroll
+                for (int x = 0; x < 8; x += 2) {  // (re, im) pairs: c0 is a multiple of 8
+                  const double cr = cold[x], ci = cold[x + 1];
+                  out[x] = fma(p.beta[0], cr, fma(-p.beta[1], ci, out[x]));
+                  out[x + 1] = fma(p.beta[0], ci, fma(p.beta[1], cr, out[x + 1]));
+                }
+              }
+            }
+            if (p.vecc && c0 + 8 <= N) {
+#pragma unroll
+              for (int x = 0; x < 8; x += 2)
+                *reinterpret_cast<double2*>(crow + c0 + x) = make_double2(out[x], out[x + 1]);
+            } else {
+#pragma unroll
+              for (int x = 0; x < 8; x++)
+                if (c0 + x < N) crow[c0 + x] = out[x];
+            }
+          }
+        }
+        tc_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[k]);
+      }
+    }
+    if (need_c) cp_async_wait<0>();
+    if (issuer) {
+      mma_commit(mfin);
+      mbar_wait_bounded(mfin, 0, nullptr);
     }
   }
-  if (!bail && nt > 0) {
-    bool ok = wait_mma(nt - 1);
-    if (__syncthreads_or(!ok)) {
-      bail = true;
-    } else {
-      tc_after();
-      epilogue(nt - 1);
-    }
-  }
-  if (bail)
-    for (int bb = 0; bb < 2; bb++)
-      if (uses[bb] > 0) mbar_wait_bounded(&bar_mma[bb], (uint32_t)((uses[bb] - 1) & 1), nullptr);
   tc_before();
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
 }  // namespace stsmm
@@ -569,54 +655,50 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   if (a.fold) a.beta_zero = 1;
   a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
   a.vecc = ((uintptr_t)C % 16 == 0) && (a.ldc % 2 == 0);
-  a.abuf = (uint32_t)(ROWS * 8 * MP * 2);  // 128 rows x 8 planes x MP x fp16
-  const int64_t bdig = round_up((int64_t)8 * MP * a.NM * 2, 1024);
-  const int64_t avail = h->dev.smem_optin - HDR - bdig;
-  a.nabuf = avail >= 2 * (int64_t)a.abuf ? 2 : 1;
-  if (avail < (int64_t)a.abuf) {
+  a.NB = a.NM == 16 ? 16 : 32;
+  a.ncb = a.NM / a.NB;
+  a.nsets = 512 / (8 * a.NB);
+  a.astage = (uint32_t)(ROWS * DIGITS * MP * 2);
+  a.bbytes = (uint32_t)round_up((int64_t)2 * DIGITS * MP * a.NM, 1024);
+  const int HDR = MP == 64 ? hdr_bytes<64>() : (MP == 32 ? hdr_bytes<32>() : hdr_bytes<16>());
+  const int64_t cbytes =
+      (int64_t)2 * (MP == 64 ? c_depth<64>() : (MP == 32 ? c_depth<32>() : c_depth<16>())) * CHUNK_BYTES;
+  // the deepest A' ring that fits beside B' and the old-C rings (one stage at MP = 64)
+  a.nast = 0;
+  for (int ns = MAXAST; ns >= 1 && a.nast == 0; ns--)
+    if (HDR + (int64_t)a.bbytes + (int64_t)ns * a.astage + cbytes <= h->dev.smem_optin) a.nast = ns;
+  if (a.nast == 0) {
     set_error("split precision TSMM: tiles do not fit in shared memory");
     return SKINNY_UNSUPPORTED;
   }
-  // two CTAs per SM where a CTA fits half the TMEM and half the shared memory (contraction width
-  // 16: 128 registers); otherwise one CTA with two accumulator sets where they fit
-  const int smem_need = (int)(HDR + bdig + (int64_t)a.nabuf * a.abuf);
-  const bool two = MP <= 16 && 8 * a.NM <= 256 && 2 * smem_need <= h->dev.smem_optin;
-  a.ntbuf = two ? 256 / (8 * a.NM) : (2 * 8 * a.NM <= 512 ? 2 : 1);
-  a.tmem_cols = two ? 256 : (a.ntbuf * 8 * a.NM <= 256 ? 256 : 512);
   a.ntiles = (K + ROWS - 1) / ROWS;
+  // without old C the epilogue has slack: it issues the MMAs, la tiles ahead, where the sets allow
+  // and a tile takes few MMAs (contraction width 16: 8; measured slower at 32, whose 16 MMAs per
+  // tile hold the issuing epilogue warp too long)
+  a.la = (a.beta_zero && MP == 16 && a.nsets >= 2 * a.ncb) ? a.nsets / a.ncb - 1 : 0;
   a.err = h->err;
-  const int smem = (int)(HDR + bdig + (int64_t)a.nabuf * a.abuf);
-  const int per_sm = two ? 2 : 1;
-  int64_t grid = std::min<int64_t>((int64_t)h->dev.sms * per_sm, a.ntiles);
+  const int smem = (int)(HDR + (int64_t)a.bbytes + (int64_t)a.nast * a.astage + cbytes);
+  int64_t grid = std::min<int64_t>((int64_t)h->dev.sms, a.ntiles);
   if (grid < 1) grid = 1;
-  cudaError_t e;
+  static SmemAttr attr16, attr32, attr64;
+  bool attr_ok;
   switch (MP) {
     case 16:
-      if (two) {
-        static SmemAttr attr;
-        ensure_smem_attr(split_tsmm_kernel<16, 256>, smem, attr);
-        split_tsmm_kernel<16, 256><<<(int)grid, 256, smem, st>>>(a);
-      } else {
-        static SmemAttr attr;
-        ensure_smem_attr(split_tsmm_kernel<16, 512>, smem, attr);
-        split_tsmm_kernel<16, 512><<<(int)grid, 512, smem, st>>>(a);
-      }
+      attr_ok = ensure_smem_attr(split_tsmm_kernel<16>, smem, attr16);
+      if (attr_ok) split_tsmm_kernel<16><<<(int)grid, THREADS, smem, st>>>(a);
       break;
-    case 32: {
-      static SmemAttr attr;
-      ensure_smem_attr(split_tsmm_kernel<32, 512>, smem, attr);
-      split_tsmm_kernel<32, 512><<<(int)grid, 512, smem, st>>>(a);
+    case 32:
+      attr_ok = ensure_smem_attr(split_tsmm_kernel<32>, smem, attr32);
+      if (attr_ok) split_tsmm_kernel<32><<<(int)grid, THREADS, smem, st>>>(a);
       break;
-    }
-    default: {
-      static SmemAttr attr;
-      ensure_smem_attr(split_tsmm_kernel<64, 512>, smem, attr);
-      split_tsmm_kernel<64, 512><<<(int)grid, 512, smem, st>>>(a);
+    default:
+      attr_ok = ensure_smem_attr(split_tsmm_kernel<64>, smem, attr64);
+      if (attr_ok) split_tsmm_kernel<64><<<(int)grid, THREADS, smem, st>>>(a);
       break;
-    }
   }
+  if (!attr_ok) return SKINNY_DEVICE_ERROR;  // the error text is set
   count_launch();
-  e = cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("split tsmm launch: ") + cudaGetErrorString(e));
     return SKINNY_DEVICE_ERROR;
