@@ -327,8 +327,9 @@ def kernel_of(it, method):
 
 def call(h, it, ops, i, method):
     M, N, K = it["M"], it["N"], it["K"]
-    # FP64 and complex FP64 take the method (split covers complex TSMM); dd is real FP64 only
-    acc = method if it["dt"] == "f64" or (it["dt"] == "c64" and method != "dd") else "native"
+    # FP64 and complex FP64 take the method (split covers complex TSMM); dd covers every dtype,
+    # split FP64 and complex FP64 only
+    acc = method if it["dt"] in ("f64", "c64") or method == "dd" else "native"
     if it["op"] == "tsmm":
         ld_c = M if it["inplace"] else N
         h.tsmm(M, N, K, ops["A"][0], M, 1.0, ops["B"][0], M, 0.5, ops["C"], ld_c, acc=acc)

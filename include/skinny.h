@@ -58,7 +58,9 @@ typedef enum {
 
 typedef enum {
   SKINNY_ACC_NATIVE = 0, /* accumulate in the working type (reference dItype == dtype) */
-  SKINNY_ACC_DD = 1,     /* double-double accumulation, R64 only (reference dItype == PseudoQuad, types.hpp:49-57) */
+  SKINNY_ACC_DD = 1,     /* exact-product accumulation: R64 double-double (reference dItype == PseudoQuad,
+                            types.hpp:49-57), C64 double-double real and imaginary parts, R32 / C32 in
+                            FP64 / complex FP64; not for the conjugate product */
   SKINNY_ACC_SPLIT = 2,  /* R64 split precision: FP64 sliced into BF16 digits, products on tcgen05
                             tensor cores with exact FP32 accumulation, recombined in FP64.  No
                             counterpart in the reference. */

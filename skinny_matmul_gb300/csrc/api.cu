@@ -12,6 +12,20 @@
 #include "launch.cuh"
 
 namespace skinny {
+// instantiated in the inst_*.cu units
+SKINNY_LAUNCHERS(extern, float, float)
+SKINNY_LAUNCHERS(extern, double, double)
+SKINNY_LAUNCHERS(extern, double, dd)
+SKINNY_LAUNCHERS(extern, c32, c32)
+SKINNY_LAUNCHERS(extern, c64, c64)
+SKINNY_LAUNCHERS(extern, c32h, c32h)
+SKINNY_LAUNCHERS(extern, c64h, c64h)
+SKINNY_LAUNCHERS(extern, float, double)
+SKINNY_LAUNCHERS(extern, c32, c64)
+SKINNY_LAUNCHERS(extern, c64, zdd)
+}  // namespace skinny
+
+namespace skinny {
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
@@ -232,6 +246,8 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
                                void* C, int64_t ldc, cudaStream_t st, const LaunchOpts& o) {
   switch (dt) {
     case SKINNY_R32:
+      if (acc == SKINNY_ACC_DD)  // FP64 accumulation of exact products
+        return run_t<float, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<float, float>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
@@ -249,10 +265,14 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
       }
       return run_t<double, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
     case SKINNY_C32:
+      if (acc == SKINNY_ACC_DD)  // complex FP64 accumulation of exact products
+        return run_t<c32, c64>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<c32, c32>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
     case SKINNY_C64:
+      if (acc == SKINNY_ACC_DD)  // double-double real and imaginary parts
+        return run_t<c64, zdd>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       if (acc == SKINNY_ACC_SPLIT || (acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_NATIVE)) {
         const bool autosel = acc == SKINNY_ACC_AUTO && o.method != SKINNY_ACC_SPLIT;
         skinny_status s =

@@ -29,6 +29,7 @@ struct __align__(2 * sizeof(R)) cplxh {
 };
 typedef cplxh<float> c32h;
 typedef cplxh<double> c64h;
+typedef cplx<dd> zdd;  // double-double real and imaginary parts
 
 // One entry of alpha*B + beta*I (in-place TSMM with M == N: C = A (alpha B + beta I)): alpha*b,
 // plus beta on the diagonal (one rounding for real types)
@@ -192,6 +193,91 @@ struct Ops<double, dd> {  // double inputs, PseudoQuad accumulation
   static __device__ __forceinline__ bool is_one(double) { return false; }
   static __device__ __forceinline__ dd shfl_xor(dd v, int o) {
     return {__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.t, o)};
+  }
+};
+
+// The double-double method for the other dtypes (the reference defines PseudoQuad accumulation
+// for real FP64 only, types.hpp:49-57): an accumulator in which every product is exact --
+// FP64 for FP32 data (a product of two floats fits a double), complex FP64 for complex FP32, and
+// PseudoQuad real and imaginary parts for complex FP64 (axpy2 per real product, accu to merge).
+// The result is rounded once to the storage type after alpha and beta are applied in the
+// accumulator's precision (beta * C in the storage precision's double for complex FP64, as the
+// real double-double method does).
+template <>
+struct Ops<float, double> {
+  static __device__ __forceinline__ double zero() { return 0.0; }
+  static __device__ __forceinline__ double mac(double acc, float a, float b) {
+    return fma((double)a, (double)b, acc);
+  }
+  static __device__ __forceinline__ double add(double x, double y) { return x + y; }
+  static __device__ __forceinline__ float finish(double s, float alpha, float beta, bool beta_zero, const float* c) {
+    const double v = (double)alpha * s;
+    return (float)(beta_zero ? v : fma((double)*c, (double)beta, v));
+  }
+  static __device__ __forceinline__ float finish1(double s, float beta, bool beta_zero, const float* c) {
+    return (float)(beta_zero ? s : fma((double)*c, (double)beta, s));
+  }
+  static __device__ __forceinline__ bool is_one(float a) { return a == 1.0f; }
+  static __device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+};
+
+template <>
+struct Ops<c32, c64> {
+  static __device__ __forceinline__ c64 zero() { return {0.0, 0.0}; }
+  static __device__ __forceinline__ c64 mac(c64 acc, c32 a, c32 b) {
+    const double ax = a.x, ay = a.y, bx = b.x, by = b.y;
+    acc.x = fma(ax, bx, acc.x);
+    acc.x = fma(-ay, by, acc.x);
+    acc.y = fma(ax, by, acc.y);
+    acc.y = fma(ay, bx, acc.y);
+    return acc;
+  }
+  static __device__ __forceinline__ c64 add(c64 x, c64 y) { return {x.x + y.x, x.y + y.y}; }
+  static __device__ __forceinline__ c32 finish(c64 s, c32 alpha, c32 beta, bool beta_zero, const c32* c) {
+    const double ar = alpha.x, ai = alpha.y;
+    double vr = fma(ar, s.x, -ai * s.y), vi = fma(ar, s.y, ai * s.x);
+    if (!beta_zero) {
+      const double br = beta.x, bi = beta.y, cr = c->x, ci = c->y;
+      vr += fma(br, cr, -bi * ci);
+      vi += fma(br, ci, bi * cr);
+    }
+    return {(float)vr, (float)vi};
+  }
+  static __device__ __forceinline__ c32 finish1(c64 s, c32 beta, bool beta_zero, const c32* c) {
+    return finish(s, {1.0f, 0.0f}, beta, beta_zero, c);
+  }
+  static __device__ __forceinline__ bool is_one(c32 a) { return a.x == 1.0f && a.y == 0.0f; }
+  static __device__ __forceinline__ c64 shfl_xor(c64 v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)};
+  }
+};
+
+template <>
+struct Ops<c64, zdd> {
+  static __device__ __forceinline__ zdd zero() { return {{0.0, 0.0}, {0.0, 0.0}}; }
+  static __device__ __forceinline__ zdd mac(zdd acc, c64 a, c64 b) {
+    acc.x = dd_axpy2(acc.x, a.x, b.x);
+    acc.x = dd_axpy2(acc.x, -a.y, b.y);
+    acc.y = dd_axpy2(acc.y, a.x, b.y);
+    acc.y = dd_axpy2(acc.y, a.y, b.x);
+    return acc;
+  }
+  static __device__ __forceinline__ zdd add(zdd x, zdd y) { return {dd_accu(x.x, y.x), dd_accu(x.y, y.y)}; }
+  static __device__ __forceinline__ c64 finish(zdd s, c64 alpha, c64 beta, bool beta_zero, const c64* c) {
+    const dd sr = dd_fast2sum(s.x.s, s.x.t), si = dd_fast2sum(s.y.s, s.y.t);  // renormalize
+    const dd re = dd_accu(dd_scale2(sr, alpha.x), dd_scale2(si, -alpha.y));
+    const dd im = dd_accu(dd_scale2(sr, alpha.y), dd_scale2(si, alpha.x));
+    const double vr = __dadd_rn(re.s, re.t), vi = __dadd_rn(im.s, im.t);  // convert
+    if (beta_zero) return {vr, vi};
+    return {__dadd_rn(__fma_rn(beta.x, c->x, -beta.y * c->y), vr), __dadd_rn(__fma_rn(beta.x, c->y, beta.y * c->x), vi)};
+  }
+  static __device__ __forceinline__ c64 finish1(zdd s, c64 beta, bool beta_zero, const c64* c) {
+    return finish(s, {1.0, 0.0}, beta, beta_zero, c);
+  }
+  static __device__ __forceinline__ bool is_one(c64) { return false; }
+  static __device__ __forceinline__ zdd shfl_xor(zdd v, int o) {
+    return {{__shfl_xor_sync(0xffffffffu, v.x.s, o), __shfl_xor_sync(0xffffffffu, v.x.t, o)},
+            {__shfl_xor_sync(0xffffffffu, v.y.s, o), __shfl_xor_sync(0xffffffffu, v.y.t, o)}};
   }
 };
 

@@ -1,12 +1,8 @@
-// inst_dd.cu -- explicit instantiation of the CUDA-core TSMTTSM / TSMM launchers for
-// storage type double with accumulator dd (one translation unit per type so the build runs in parallel).
+// inst_dd.cu -- explicit instantiation of the CUDA-core TSMTTSM / TSMM launchers for storage type
+// double with accumulator dd (the double-double method) (one translation unit per type pair, so
+// that the build runs in parallel).
 #include "launch.cuh"
 
 namespace skinny {
-template skinny_status tsmttsm_run<double, dd>(const DeviceInfo&, Workspace&, int*, cudaStream_t, int64_t,
-                                          int64_t, int64_t, const double*, int64_t, double, const double*,
-                                          int64_t, double, bool, double*, int64_t, const LaunchOpts&);
-template skinny_status tsmm_run<double, dd>(const DeviceInfo&, cudaStream_t, int64_t, int64_t, int64_t,
-                                       const double*, int64_t, double, const double*, int64_t, double, bool, double*,
-                                       int64_t, const LaunchOpts&);
+SKINNY_LAUNCHERS(, double, dd)
 }  // namespace skinny

@@ -97,18 +97,23 @@ skinny_status tsmttsm_launch_tile(const TsmttsmArgs<T>& a, dim3 grid, int smem, 
   return SKINNY_OK;
 }
 
+// Register-tile entries (accumulators) a thread of the ring kernel may hold: 64 FP64-sized ones,
+// 32 of 16 bytes, 8 of 32 bytes (complex double-double)
+template <typename Acc>
+constexpr int tile_cap() {
+  return sizeof(Acc) >= 32 ? 8 : (int)(128 / (sizeof(Acc) / 4));
+}
+
 template <typename T, typename Acc>
 skinny_status tsmttsm_dispatch(int tm, int tn, const TsmttsmArgs<T>& a, dim3 grid, int smem,
                                cudaStream_t st) {
-#define SK_TILE(X, Y) \
-  if (tm == X && tn == Y) return tsmttsm_launch_tile<T, Acc, X, Y>(a, grid, smem, st);
+#define SK_TILE(X, Y)                                                                   \
+  if constexpr (X * Y <= tile_cap<Acc>() && X * Y <= 64)                                \
+    if (tm == X && tn == Y) return tsmttsm_launch_tile<T, Acc, X, Y>(a, grid, smem, st);
   SK_TILE(1, 1) SK_TILE(1, 2) SK_TILE(1, 4) SK_TILE(1, 8)
   SK_TILE(2, 1) SK_TILE(2, 2) SK_TILE(2, 4) SK_TILE(2, 8)
   SK_TILE(4, 1) SK_TILE(4, 2) SK_TILE(4, 4) SK_TILE(4, 8)
-  SK_TILE(8, 1) SK_TILE(8, 2) SK_TILE(8, 4)
-  if constexpr (sizeof(Acc) <= 8) {
-    SK_TILE(8, 8)
-  }
+  SK_TILE(8, 1) SK_TILE(8, 2) SK_TILE(8, 4) SK_TILE(8, 8)
 #undef SK_TILE
   set_error("tsmttsm: no compiled register tile");
   return SKINNY_UNSUPPORTED;
@@ -124,7 +129,7 @@ template <typename T, typename Acc>
 skinny_status tsmttsm_plan(const DeviceInfo& dev, int64_t M, int64_t N, int64_t K, const void* A,
                            int64_t lda, const void* B, int64_t ldb, bool gram, const LaunchOpts& o,
                            TsmttsmPlan& pl) {
-  const int cap = (int)(128 / (sizeof(Acc) / 4));
+  const int cap = tile_cap<Acc>();
   int tm = pow2ceil(M) < 8 ? pow2ceil(M) : 8;
   int tn = pow2ceil(N) < 8 ? pow2ceil(N) : 8;
   while (tm * tn > cap) (tm >= tn ? tm : tn) /= 2;
@@ -186,10 +191,11 @@ skinny_status tsmttsm_plan(const DeviceInfo& dev, int64_t M, int64_t N, int64_t 
 
 // ----------------------------------------------------------------- TSMTTSM, narrow products
 // Register-tile entries a thread of the row-streaming kernel may hold: 64 for 4- and 8-byte
-// accumulators (FP64 8 x 8), 16 for 16-byte ones (complex FP64, double-double).
+// accumulators (FP64 8 x 8), 16 for 16-byte ones (complex FP64, double-double), 4 for 32-byte
+// ones (complex double-double).
 template <typename Acc>
 constexpr int rows_cap() {
-  return sizeof(Acc) <= 8 ? 64 : 16;
+  return sizeof(Acc) <= 8 ? 64 : (sizeof(Acc) <= 16 ? 16 : 4);
 }
 
 // The row-streaming kernel takes a product when both padded widths are <= 8 and their tile fits
@@ -344,7 +350,7 @@ template <typename T, typename Acc>
 skinny_status tsmm_run(const DeviceInfo& dev, cudaStream_t st, int64_t M, int64_t N, int64_t K,
                        const T* A, int64_t lda, T alpha, const T* B, int64_t ldb, T beta,
                        bool beta_zero, T* C, int64_t ldc, const LaunchOpts& o) {
-  const int cap = sizeof(Acc) <= 8 ? 8 : 4;
+  const int cap = sizeof(Acc) <= 8 ? 8 : (sizeof(Acc) <= 16 ? 4 : 2);
   int tn = pow2ceil(N) < cap ? pow2ceil(N) : cap;
   int gn = pow2ceil((N + tn - 1) / tn);
   if (gn > 32) {
@@ -376,22 +382,39 @@ skinny_status tsmm_run(const DeviceInfo& dev, cudaStream_t st, int64_t M, int64_
   a.np = np;
   const int sm = (int)(smem < 16 ? 16 : smem);
   // narrow rows (M <= 4, a few outputs per thread): 4 rows per thread and step
-  const bool multi = M <= 4 && tn <= 4;
+  // (32-byte accumulators: one row per thread and step)
+  const bool multi = M <= 4 && tn <= 4 && sizeof(Acc) <= 16;
   switch (tn) {
     case 1:
-      return multi ? tsmm_launch_tile<T, Acc, 1, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
-                   : tsmm_launch_tile<T, Acc, 1, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+      if constexpr (sizeof(Acc) <= 16)
+        if (multi) return tsmm_launch_tile<T, Acc, 1, 4>(a, o.blocks_per_sm, dev.sms, sm, st);
+      return tsmm_launch_tile<T, Acc, 1, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
     case 2:
-      return multi ? tsmm_launch_tile<T, Acc, 2, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
-                   : tsmm_launch_tile<T, Acc, 2, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+      if constexpr (sizeof(Acc) <= 16)
+        if (multi) return tsmm_launch_tile<T, Acc, 2, 4>(a, o.blocks_per_sm, dev.sms, sm, st);
+      return tsmm_launch_tile<T, Acc, 2, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
     case 4:
-      return multi ? tsmm_launch_tile<T, Acc, 4, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
-                   : tsmm_launch_tile<T, Acc, 4, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+      if constexpr (sizeof(Acc) <= 16) {
+        return multi ? tsmm_launch_tile<T, Acc, 4, 4>(a, o.blocks_per_sm, dev.sms, sm, st)
+                     : tsmm_launch_tile<T, Acc, 4, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
+      }
+      break;
     default:
       if constexpr (sizeof(Acc) <= 8) return tsmm_launch_tile<T, Acc, 8, 1>(a, o.blocks_per_sm, dev.sms, sm, st);
   }
   set_error("tsmm: no compiled column tile");
   return SKINNY_UNSUPPORTED;
 }
+
+// Explicit instantiation of both launchers for a (storage, accumulator) pair (EXT empty: the
+// inst_*.cu units, one pair or two each, so that the build compiles them in parallel) or its
+// extern declaration (EXT extern: the units that call them).
+#define SKINNY_LAUNCHERS(EXT, T, ACC)                                                                         \
+  EXT template skinny_status tsmttsm_run<T, ACC>(const DeviceInfo&, Workspace&, int*, cudaStream_t, int64_t, \
+                                                 int64_t, int64_t, const T*, int64_t, T, const T*, int64_t, T, \
+                                                 bool, T*, int64_t, const LaunchOpts&);                      \
+  EXT template skinny_status tsmm_run<T, ACC>(const DeviceInfo&, cudaStream_t, int64_t, int64_t, int64_t,     \
+                                              const T*, int64_t, T, const T*, int64_t, T, bool, T*, int64_t,   \
+                                              const LaunchOpts&);
 
 }  // namespace skinny

@@ -224,7 +224,19 @@ __device__ __forceinline__ long long level_window(const uint32_t (&raw)[8][8], i
   }
   const int P1 = d[0] * 256 + d[1], P2 = d[2] * 256 + d[3];
   const int P3 = d[4] * 256 + d[5], P4 = d[6] * 256 + d[7];
-  return ((long long)P1 << 36) + (long long)P2 * (1 << 20) + (long long)P3 * 16 + (long long)(P4 >> 12);
+  // W = P1 2^36 + P2 2^20 + P3 2^4 + (P4 >> 12): two wide multiply-adds, then P1 * 16 into the
+  // high word (the sum wraps modulo 2^64 harmlessly: |W| < 2^62)
+  long long w;
+  asm("{\n .reg .s64 t;\n .reg .b32 lo, hi;\n"
+      " cvt.s64.s32 t, %4;\n"
+      " mad.wide.s32 t, %3, 16, t;\n"
+      " mad.wide.s32 t, %2, 1048576, t;\n"
+      " mov.b64 {lo, hi}, t;\n"
+      " mad.lo.s32 hi, %1, 16, hi;\n"
+      " mov.b64 %0, {lo, hi};\n}"
+      : "=l"(w)
+      : "r"(P1), "r"(P2), "r"(P3), "r"(P4 >> 12));
+  return w;
 }
 // Integer finisher, ex = er + fc - 1014 (the biased exponent field of the result when W has its
 // leading one at bit 63): normalise |W| so that its leading one is bit 63, round on bit 10 (ties
@@ -462,15 +474,16 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     // the FP64-pipe finisher where the epilogue runs no beta FMA on that pipe (measured: with the
     // FMA, the conversion makes the FP64 pipe the bottleneck even on one warp group)
     const bool cvt = !need_c;
-    const int64_t gtot = (int64_t)nt * CHg;
-    // old C of this warp's chunk g (tile g / CHg, chunk eg + 2 (g % CHg)) into ring slot g % CD
-    auto issue = [&](int64_t g) {
-      if (g < gtot) {
-        const int it = (int)(g / CHg), c = eg + 2 * (int)(g % CHg);
-        const int64_t rr = (t_begin + it) * ROWS + r;
+    // old C prefetch cursor: this warp's next chunk (tile pf_it, chunk pf_c) goes to ring slot
+    // pf_g % CD; one commit group per chunk (empty past the last chunk)
+    int pf_it = 0, pf_c = eg, pf_g = 0;
+    auto issue = [&]() {
+      if (pf_it < nt && CHg > 0) {
+        const int c = pf_c;
+        const int64_t rr = (t_begin + pf_it) * ROWS + r;
         const bool live = rr < p.K;
         const double* src = p.C + rr * p.ldc + 8 * c;
-        unsigned char* dst = cbuf + (size_t)(eg * CD + (int)(g % CD)) * CHUNK_BYTES + r * 64;
+        unsigned char* dst = cbuf + (size_t)(eg * CD + pf_g % CD) * CHUNK_BYTES + r * 64;
         if (p.vecc) {
 #pragma unroll
           for (int x = 0; x < 4; x++) {
@@ -485,15 +498,21 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
             cp_async8(dst + 8 * x, bytes ? (const void*)(src + x) : (const void*)p.C, bytes);
           }
         }
+        pf_c += 2;
+        if (pf_c >= CH) {
+          pf_c = eg;
+          pf_it++;
+        }
       }
       cp_async_commit();
+      pf_g++;
     };
     if (need_c)
-      for (int g = 0; g < CD - 1; g++) issue(g);
+      for (int i = 0; i < CD - 1; i++) issue();
     const bool issuer = p.la > 0 && warp == NSLW;
     if (issuer)
       for (int j = 0; j < p.la && j < nt; j++) issue_tile(j);
-    int64_t g = 0;
+    int g = 0;  // this warp's chunks consumed so far
     int job = 0;
     bool ok = true;
     for (int it = 0; it < nt && ok; it++) {
@@ -521,7 +540,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
         const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(k * 8 * NB);
         const int c_hi = min(CH, (cb + 1) * cpb);
         for (int c = cb * cpb + eg; c < c_hi; c += 2, g++) {
-          if (need_c) issue(g + CD - 1);  // into the slot of chunk g - 1, read in full already
+          if (need_c) issue();  // chunk g + CD - 1, into the slot of chunk g - 1, read in full already
           uint32_t raw[8][8];
 #pragma unroll
           for (int L = 0; L < 8; L++) tmem_ld8(tb + (uint32_t)(L * NB + 8 * (c - cb * cpb)), raw[L]);
@@ -529,7 +548,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
           if (need_c) {
             cp_async_wait<CD - 1>();  // this thread's copies of chunk g have landed
             const double2* cs =
-                reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + (int)(g % CD)) * CHUNK_BYTES + r * 64);
+                reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + g % CD) * CHUNK_BYTES + r * 64);
 #pragma unroll
             for (int x = 0; x < 4; x++) {
               const double2 w = cs[x];
@@ -542,13 +561,15 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
             // all eight columns are formed (columns beyond N hold zero digits and exponent 0) and
             // masked only at the store
             const int c0 = 8 * c;
+            const int4 f0 = *reinterpret_cast<const int4*>(fcol + c0), f1 = *reinterpret_cast<const int4*>(fcol + c0 + 4);
+            const int fc[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
             double out[8];
             if (cvt) {
 #pragma unroll
-              for (int x = 0; x < 8; x++) out[x] = window_cvt(level_window<MP>(raw, x), e + fcol[c0 + x] - 1086);
+              for (int x = 0; x < 8; x++) out[x] = window_cvt(level_window<MP>(raw, x), e + fc[x] - 1086);
             } else {
 #pragma unroll
-              for (int x = 0; x < 8; x++) out[x] = window_int(level_window<MP>(raw, x), e + fcol[c0 + x]);
+              for (int x = 0; x < 8; x++) out[x] = window_int(level_window<MP>(raw, x), e + fc[x]);
             }
             if (need_c) {
               if (!p.cplx || p.beta[1] == 0.0) {  // a real beta scales both parts of a complex C alike

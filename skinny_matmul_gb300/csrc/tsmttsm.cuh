@@ -87,6 +87,10 @@ __device__ __forceinline__ dd ldcg(const dd* p) {
   double2 v = __ldcg(reinterpret_cast<const double2*>(p));
   return {v.x, v.y};
 }
+__device__ __forceinline__ zdd ldcg(const zdd* p) {
+  const double2 a = __ldcg(reinterpret_cast<const double2*>(p)), b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+  return {{a.x, a.y}, {b.x, b.y}};
+}
 
 constexpr int TSMTTSM_THREADS = 256;
 constexpr int SMEM_HEADER = 128;  // mbarriers live here

@@ -4,7 +4,9 @@ Bars (written into each assertion):
   * golden integer cases (test.cu fixture design): bit-exact, every dtype and method;
   * random data: normwise error ||C - C*||_F / || |alpha| |A|^T|B| + |beta| |C0| ||_F <= 8 sqrt(K) u
     (K for TSMTTSM, M for TSMM; u = 2^-24 float, 2^-53 double) against the exact oracle;
-  * double-double accumulation: within the output rounding of the exact result (<= 2^-52 normwise).
+  * double-double accumulation: within the output rounding of the exact result (<= 2^-52 normwise
+    for FP64, 2^-51 complex FP64, 2^-23 FP32 and complex FP32, whose double-double method is FP64
+    accumulation of exact products).
 """
 import math
 
@@ -30,8 +32,15 @@ def host(t):
     return t.cpu().numpy()
 
 
-REAL = [(np.float32, "native"), (np.float64, "native"), (np.float64, "dd")]
-CPLX = [(np.complex64, "native"), (np.complex128, "native")]
+REAL = [(np.float32, "native"), (np.float64, "native"), (np.float64, "dd"), (np.float32, "dd")]
+CPLX = [(np.complex64, "native"), (np.complex128, "native"), (np.complex64, "dd"), (np.complex128, "dd")]
+
+
+def dd_bound(dt):
+    """The double-double method rounds once to the storage type at the end: FP32 and complex FP32
+    (FP64 accumulation of exact products) within a float's rounding, FP64 within 2^-52, complex
+    FP64 within 2^-51 (the complex alpha and beta products add two roundings)."""
+    return {np.float32: 2.0 ** -23, np.complex64: 2.0 ** -23, np.float64: 2.0 ** -52, np.complex128: 2.0 ** -51}[dt]
 
 
 def run(handle, op, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, acc="native", stream=None):
@@ -104,7 +113,7 @@ def test_tsmttsm_random_vs_oracle(handle, M, N, K, dt, acc):
     got = host(Cd)
     exp, den = common.tsmttsm_expected(M, N, K, A, lda, B, ldb, C0, ldc, alpha, beta)
     err = common.normwise(got, exp, den, common.c_mask_tsmttsm(M, N, ldc))
-    bound = 2.0 ** -52 if acc == "dd" else common.tol(dt, K)
+    bound = dd_bound(dt) if acc == "dd" else common.tol(dt, K)
     assert err <= bound, (err, bound)
     # padding between columns of C untouched
     mask = ~common.c_mask_tsmttsm(M, N, ldc)
@@ -135,7 +144,7 @@ def test_tsmm_random_vs_oracle(handle, M, N, dt, acc, inplace):
     got = host(Cd)
     exp, den = common.tsmm_expected(M, N, K, C0 if inplace else A, lda, B, ldb, C0, ldc, alpha, beta)
     err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
-    bound = 2.0 ** -52 if acc == "dd" else common.tol(dt, M)
+    bound = dd_bound(dt) if acc == "dd" else common.tol(dt, M)
     assert err <= bound, (err, bound)
 
 
@@ -211,6 +220,47 @@ def test_kat_on_gpu(handle):
     assert abs(host(out)[0] - hi) <= 2 * np.spacing(hi)
 
 
+@pytest.mark.parametrize("dt", [np.float32, np.complex64, np.complex128])
+def test_dd_cancellation(handle, dt):
+    """Sums that cancel to 1e-4 of their terms' magnitude.  FP32 and complex FP32: FP64
+    accumulation of exact products, so the double-double method returns the exact value rounded
+    to the storage type (within one unit), far closer than the native accumulation.  Complex FP64:
+    PseudoQuad per component keeps the reference's axpy2, which loses about u |a b| on a cancelling
+    step, so its result is held to the normwise bound and to at most the native error."""
+    rng = np.random.default_rng(7)
+    K = 50000
+    a = common.uniform(rng, K, dt)
+    b = common.uniform(rng, K, dt)
+    cplx = np.iscomplexobj(a)
+    # make sum(a * b) small: set the last term so that the float64 sum nearly cancels
+    s = np.sum(a[:-1].astype(np.complex128) * b[:-1])
+    last = -(s - 1e-4 * (1 + 1j)) / a[-1]
+    b[-1] = (last if cplx else last.real).astype(dt)
+    exp, den = common.tsmttsm_expected(1, 1, K, a, 1, b, 1, np.zeros(1, dt), 1, 1.0, 0.0)
+    out = {}
+    for acc in ("dd", "native"):
+        o = dev(np.zeros(1, dt))
+        handle.tsmttsm(1, 1, K, dev(a), 1, 1.0, dev(b), 1, 0.0, o, 1, acc=acc)
+        out[acc] = host(o).astype(np.complex128)[0]
+    e = complex(exp[0])
+    err_dd, err_n = abs(out["dd"] - e), abs(out["native"] - e)
+    if dt in (np.float32, np.complex64):
+        ulp = float(np.spacing(np.abs(np.array([e.real, e.imag], dtype=np.float32))).max())
+        assert err_dd <= 2 * ulp, (err_dd, ulp)
+        assert err_dd < 0.5 * err_n, (err_dd, err_n)
+    else:
+        assert err_dd / float(den[0]) <= dd_bound(dt), (err_dd, den[0])
+        assert err_dd <= err_n, (err_dd, err_n)
+    # TSMM 1 x 1 (C = A b over K rows is elementwise) and TSMM with the data as one long row
+    M = 64
+    A2 = common.uniform(rng, (K // M) * M, dt)
+    B2 = common.uniform(rng, M, dt)
+    C2 = dev(np.zeros(K // M, dt))
+    handle.tsmm(M, 1, K // M, dev(A2), M, 1.0, dev(B2), M, 0.0, C2, 1, acc="dd")
+    exp2, den2 = common.tsmm_expected(M, 1, K // M, A2, M, B2, M, np.zeros(K // M, dt), 1, 1.0, 0.0)
+    assert common.normwise(host(C2), exp2, den2) <= dd_bound(dt)
+
+
 def test_edge_k_zero_and_beta_zero_nan(handle):
     M, N = 4, 3
     C0 = np.arange(M * N, dtype=np.float64) + 1
@@ -271,6 +321,6 @@ def test_bad_arguments(handle):
         handle.tsmttsm(4, 4, 8, X, 4, 1.0, X, 4, 0.0, X, 4)  # C aliases A
     with pytest.raises(SkinnyError, match="BAD_ARG"):
         handle.tsmttsm(4, 4, 8, X, 3, 1.0, X[32:], 4, 0.0, X[16:], 4)  # lda < M
-    with pytest.raises(SkinnyError, match="UNSUPPORTED"):
-        handle.tsmttsm(4, 4, 8, dev(np.zeros(64, np.float32)), 4, 1.0, dev(np.zeros(64, np.float32)), 4, 0.0,
-                       dev(np.zeros(16, np.float32)), 4, acc="dd")
+    with pytest.raises(SkinnyError, match="UNSUPPORTED"):  # no double-double conjugate product
+        handle.tsmttsm(4, 4, 8, dev(np.zeros(64, np.complex64)), 4, 1.0, dev(np.zeros(64, np.complex64)), 4, 0.0,
+                       dev(np.zeros(16, np.complex64)), 4, acc="dd", conj=True)
