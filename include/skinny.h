@@ -127,6 +127,16 @@ skinny_status skinny_tsmttsm_conj(skinny_handle handle, skinny_dtype dtype, skin
 skinny_status skinny_svqb(skinny_handle handle, skinny_acc gram_acc, int64_t K, int64_t M,
                           double* X, int64_t ldx, double* orth_err_out, void* stream);
 
+/* SVQB in double-double on the host: the reference's high-precision study (svqb/svqb.cu:132-182,
+ * svqb_xd<dd_real> through MPACK's Rgemm / Rsyev), an accuracy baseline for skinny_svqb.
+ * X (input) and Q (output) are HOST arrays, K x M row-major (ld = M), M <= 256; the Gram
+ * S = X^T X, the scaling D^-1/2 (0 where S_ii <= 2^-104), the eigensolve (cyclic Jacobi in place of
+ * Rsyev; ascending eigenvalues, each vector's largest entry positive), T = D U Lambda^-1/2 and
+ * Q = X T all run in double-double arithmetic on `threads` host threads (<= 0: all hardware
+ * threads); Q is rounded to double once.  Touches no GPU.  orth_err_out (nullable):
+ * ||Q^T Q - I||_F of the rounded Q with a double-double Gram. */
+skinny_status skinny_svqb_host_dd(const double* X, double* Q, int64_t K, int M, int threads, double* orth_err_out);
+
 /* CholQR (passes = 1) / CholQR2 (passes = 2) of X (K x M, FP64, M <= 64) in place: per pass the
  * Gram S = X^T X (method gram_acc), the Cholesky S = R^T R and X <- X R^-1 by the in-place TSMM,
  * all on the device.  No counterpart in the reference (its orthogonalisation is SVQB); the same

@@ -5,7 +5,7 @@ A is C), in float / double / complex float / complex double, with double-double 
 an FP64 split-precision tensor-core path; SVQB orthogonalisation on top.  The compute runs in
 libskinny.so (include/skinny.h); this package binds it and mirrors the reference's launcher API.
 """
-from .api import Handle, Server, default_handle, launchers, svqb, tsmm, tsmttsm  # noqa: F401
+from .api import Handle, Server, default_handle, launchers, svqb, svqb_host_dd, tsmm, tsmttsm  # noqa: F401
 from .lib import SkinnyError  # noqa: F401
 
-__all__ = ["Handle", "Server", "default_handle", "launchers", "svqb", "tsmm", "tsmttsm", "SkinnyError"]
+__all__ = ["Handle", "Server", "default_handle", "launchers", "svqb", "svqb_host_dd", "tsmm", "tsmttsm", "SkinnyError"]

@@ -177,6 +177,20 @@ def svqb(K, M, X, ldx, gram_acc="split", orth_err=True, stream=None, handle=None
     return (handle or default_handle()).svqb(K, M, X, ldx, gram_acc, orth_err, stream)
 
 
+def svqb_host_dd(X, K, M, threads=0, orth_err=True):
+    """Double-double SVQB on the host (skinny_svqb_host_dd): X a host float64 array of K x M
+    (row-major); returns (Q, ||Q^T Q - I||_F or None).  Needs no GPU."""
+    import numpy as np
+    Xc = np.ascontiguousarray(X, dtype=np.float64).reshape(-1)
+    if Xc.size < K * M:
+        raise ValueError("X holds fewer than K * M values")
+    Q = np.empty(K * M, dtype=np.float64)
+    err = ctypes.c_double(-1.0)
+    L.check(L.load().skinny_svqb_host_dd(Xc.ctypes.data, Q.ctypes.data, K, M, threads,
+                                         ctypes.byref(err) if orth_err else None))
+    return Q, (err.value if orth_err else None)
+
+
 _REF_SUFFIX = {"float32": "s", "float64": "d", "complex64": "c", "complex128": "z", "dd": "dd"}
 
 

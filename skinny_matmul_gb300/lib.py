@@ -90,6 +90,7 @@ SIGNATURES = {
     "skinny_svqb": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
     "skinny_cholqr": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _i, _vp, _vp]),
     "skinny_svqb_z": (_i, [_vp, _i, _i64, _i64, _vp, _i64, _vp, _vp]),
+    "skinny_svqb_host_dd": (_i, [_vp, _vp, _i64, _i, _i, _vp]),
     "skinny_autotune": (_i, [_vp, _i, _i, _i, _i64, _i64, _i64, _vp]),
     "skinny_tune_export": (_i, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)]),
     "skinny_tune_import": (_i, [_vp, ctypes.c_char_p]),
