@@ -10,7 +10,7 @@ shape once.  Each shape's operands are larger than L2 (129 MB), so no L2 flush i
 
 The default line also carries "split_vs_fp64" (TSMTTSM FP64 64x64, K = 2^24, s*2^e entries: plain
 FP64 vs split precision vs double-double, with errors), "tsmttsm_sweep" (the metric's TSMTTSM half:
-FP64 M = N in {1..64} with A and B of 1 GiB, and C1) and "serving" (600 requests of the serving
+FP64 M = N in {1..64} with A and B of 1 GiB, and C1) and "serving" (C5: 20000 requests of the serving
 mix through the request loop vs one launch per call); --no-extras skips them.
 
 The reference arm (--impl reference) times the oracle port of the reference's loops on the host
@@ -18,7 +18,7 @@ cores (its value) and, on the default workload, the reference's own GPU kernels 
 ("gpu_kernels": compiled from its headers into oracle/_ref, best variant and blockCount per shape).
 
 Other workloads: "tsmttsm-c1" (TSMTTSM FP64 8x8, K = 2^20, 16 rotating input copies),
-"precision-c3" (M = N in {32, 64, 128}), "svqb-c4", "serve-c5" (2000 requests), and probes for ncu.
+"precision-c3" (M = N in {32, 64, 128}), "svqb-c4", "serve-c5" (20000 requests), and probes for ncu.
 
 Byte and flop formulas follow the reference's perf harness (perf.cu:208-232):
   TSMM beta != 0: (M K + 2 N K + M N) s bytes, in place (M K + N K + M N) s; flops (MNK + NK) f
@@ -319,7 +319,7 @@ def kernel_of(it, method):
             return "tsmttsm_rows_kernel"
         return "tsmttsm_kernel"
     Mr, Nr = (2 * M, 2 * N) if it["dt"] == "c64" else (M, N)
-    auto_split = K >= 8192 and Mr * Nr >= 128 and Nr >= 8 and Mr >= 4
+    auto_split = K >= 8192 and (Mr * Nr >= 128 or (it["dt"] == "c64" and Mr * Nr >= 64)) and Nr >= 8 and Mr >= 4
     if fp64 and (method == "split" or (method == "auto" and auto_split)):
         return "split_tsmm_kernel"
     return "tsmm_kernel"
@@ -549,7 +549,7 @@ def main():
     ap.add_argument("--method", default="auto", choices=["auto", "native", "split", "dd"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--requests", type=int, default=2000, help="serve-c5: number of requests")
+    ap.add_argument("--requests", type=int, default=20000, help="serve-c5: number of requests")
     ap.add_argument("--store", default=None, help="append every measured shape to this JSONL results store")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload: skip the compact split-vs-FP64 and serving measurements")
@@ -661,7 +661,7 @@ def main():
         cpu = {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port", "sample": desc}
 
     # the metric's other two parts, measured compactly beside the sweep on the same GPU: split vs
-    # plain FP64 TSMTTSM (M = N = 64, K = 2^24, s*2^e data) and the served stream (600 requests)
+    # plain FP64 TSMTTSM (M = N = 64, K = 2^24, s*2^e data) and the served stream (C5, 20000 requests)
     extras = {}
     if args.workload == "tsmm-sweep" and world == 1 and not args.no_extras:
         del ops
@@ -678,9 +678,9 @@ def main():
             "config": "TSMTTSM FP64 C(MxM) = A^T B, M = N in {1..64}, A and B of 1 GiB each (> L2), plus C1 "
                       "(8 x 8, K = 2^20, 16 rotating copies); auto = the library's choice, native = CUDA-core FP64",
             "shapes": tsmttsm_sweep(h, dev)}
-        seq, srv, _, wall_srv = serve_measure(h, dev, 600, 2000.0, rank)
+        seq, srv, _, wall_srv = serve_measure(h, dev, 20000, 2000.0, rank)
         extras["serving"] = {
-            "config": "600 requests of the serving mix (Poisson, 2000/s), operands resident in HBM",
+            "config": "C5: 20000 requests of the serving mix (Poisson, 2000/s), operands resident in HBM",
             "served": srv, "one_launch_per_call": seq, "throughput_ratio": round(seq["wall_s"] / wall_srv, 3),
             "p99_ratio": round(srv["p99_ms"] / seq["p99_ms"], 3) if seq["p99_ms"] else None}
 
