@@ -21,16 +21,17 @@
 //     (level_window), rounded to a double (integer instructions, or the FP64 pipe's conversion
 //     when there is no beta*C) and scaled by 2^(e_r + f_n - 2100) in the exponent field; beta*C
 //     is one FMA.
-//   * Warp roles, hand-offs through mbarriers, no CTA-wide barrier while streaming:
-//       warps 0-7   slicers: two threads per row of a 128-row tile read the row's FP64 values
-//                   (the next tile's are loaded right after a tile is sliced), take the row
-//                   exponent, and write the digit planes into an A' stage; warp 0 then issues
-//                   the tile's MMAs (one elected lane): per block of NB output columns, 8 MP / 16 MMAs into
+//   * Warp roles, hand-offs through mbarriers, no CTA-wide barrier while streaming (16 warps):
+//       slicers     (8 warps, two threads per row) read the FP64 values of a 128-row tile (the
+//                   next tile's are loaded right after a tile is sliced), take the row exponent,
+//                   and write the digit planes into an A' stage; warp 0 then issues the tile's
+//                   MMAs (one elected lane): per block of NB output columns, 8 MP / 16 MMAs into
 //                   one of 2 or 4 TMEM accumulator sets, so that a block's epilogue overlaps the
 //                   next blocks' MMAs;
-//       warps 8-15  epilogue: two warps per TMEM lane quadrant (32 rows), which take alternate
-//                   chunks (8 output columns) of a block; old C values are prefetched chunk by
-//                   chunk (cp.async) into a shared-memory ring several chunks ahead.
+//       epilogue    (8 warps: 2 groups of one warp per TMEM lane quadrant) convert the level
+//                   sums; the groups take chunks of 8 output columns in turn; old C values are
+//                   prefetched chunk by chunk (cp.async) into a shared-memory ring per group,
+//                   several chunks ahead.
 //     Every wait is bounded; a wait that runs out sets the error word and every role stops at its
 //     next wait (C is then incomplete).
 //   * In place with M == N, beta is folded into the diagonal of alpha*B before slicing
@@ -50,9 +51,15 @@ namespace stsmm {
 
 constexpr int ROWS = 128;
 constexpr int DIGITS = 8;
-constexpr int NSLW = 8;                   // slicer warps 0-7 (two threads per row); warp 0 issues the MMAs
-constexpr int NEPW = 8;                   // epilogue warps 8-15 (two per TMEM lane quadrant)
-constexpr int THREADS = (NSLW + NEPW) * 32;  // 512: four warps per SM sub-partition, 128 registers
+constexpr int THREADS = 512;  // 16 warps: four per SM sub-partition, 128 registers
+// Warp roles: 8 slicer warps (two threads per row; warp 0 issues the MMAs) and 8 epilogue warps
+// (two groups of one warp per TMEM lane quadrant).  Measured and dropped at MP = 16: 4 slicer
+// warps (one thread per row) with 12 epilogue warps -- three groups split blocks of 2 or 4 chunks
+// unevenly, and the slicers fell behind (real 8 x 32 3.76 -> 4.60 ms, 16 x 16 1.14 -> 1.25 ms).
+template <int MP>
+__host__ __device__ constexpr int slicer_warps() { return 8; }
+template <int MP>
+__host__ __device__ constexpr int epi_groups() { return (16 - slicer_warps<MP>()) / 4; }
 constexpr int MAXAST = 3;                 // A' stages (at most)
 constexpr int CHUNK_BYTES = ROWS * 64;    // one chunk of old C: 8 doubles of each of 128 rows
 constexpr uint32_t SLEEP_MMA = 32;        // ns between polls of the MMA thread
@@ -284,7 +291,9 @@ __device__ __forceinline__ void cp_async_wait() {
 
 template <int MP>
 __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
-  constexpr int PART = MP / 2;         // A values per slicer thread (two threads per row)
+  constexpr int NSL = slicer_warps<MP>(), NEP = 16 - NSL, EG = epi_groups<MP>();
+  constexpr int TPS = NSL * 32 / ROWS;  // slicer threads per row (1 or 2)
+  constexpr int PART = MP / TPS;        // A values per slicer thread
   constexpr int CD = c_depth<MP>();    // old-C chunks in flight per epilogue thread
   constexpr int RE = row_ring<MP>(), HDR = hdr_bytes<MP>();
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -301,7 +310,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
   int* erow = reinterpret_cast<int*>(smem + 1024);              // [RE][ROWS] row exponents
   unsigned char* bdig = smem + HDR;                             // B' (1024-aligned)
   unsigned char* adig = bdig + p.bbytes;                        // A' stages
-  unsigned char* cbuf = adig + (size_t)p.nast * p.astage;       // [2 groups][CD][ROWS][8 doubles] old C
+  unsigned char* cbuf = adig + (size_t)p.nast * p.astage;       // [EG groups][CD][ROWS][8 doubles] old C
   const int M = p.M, N = p.N, NB = p.NB;
   // B' per block of NB output columns: rows j * NB + n (digit j + 1 of column n), K-major over
   // m in octets of 8 rows x 16 bytes (no swizzle); bytes between k-octets and between blocks:
@@ -317,16 +326,16 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
   }
   if (tid == 0) {
     for (int s = 0; s < MAXAST; s++) {
-      mbar_init(&afull[s], NSLW);
+      mbar_init(&afull[s], NSL);
       mbar_init(&aempty[s], 1);
     }
     for (int k = 0; k < 4; k++) {
       mbar_init(&tfull[k], 1);
-      mbar_init(&tempty[k], NEPW);
+      mbar_init(&tempty[k], NEP);
     }
     for (int e = 0; e < RE; e++) {
-      mbar_init(&efull[e], NSLW);
-      mbar_init(&eempty[e], NEPW);
+      mbar_init(&efull[e], NSL);
+      mbar_init(&eempty[e], NEP);
     }
     mbar_init(mfin, 1);
     *abort_f = 0;
@@ -392,9 +401,9 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     mma_commit(&aempty[s]);
     return true;
   };
-  if (warp < NSLW) {
+  if (warp < NSL) {
     // ---- slicers: row = tid / 2, columns [m0, m0 + PART) ------------------------------------
-    const int row = tid >> 1, part = tid & 1, m0 = part * PART;
+    const int row = tid / TPS, part = tid % TPS, m0 = part * PART;
     double v[PART];
     auto load_tile = [&](int it) {
       const int64_t r1 = (t_begin + it) * ROWS;
@@ -406,7 +415,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
       uint32_t emax = 0;
 #pragma unroll
       for (int j = 0; j < PART; j++) emax = max(emax, exp_field(v[j]));
-      emax = max(emax, (uint32_t)__shfl_xor_sync(0xffffffffu, emax, 1));
+      if (TPS == 2) emax = max(emax, (uint32_t)__shfl_xor_sync(0xffffffffu, emax, 1));
       bool ok = *abort_f == 0;
       if (ok && it >= RE) ok = wait_ab(&eempty[es], (uint32_t)((it / RE - 1) & 1), abort_f, p.err);
       if (ok && it >= p.nast) ok = wait_ab(&aempty[s], (uint32_t)((it / p.nast - 1) & 1), abort_f, p.err);
@@ -453,10 +462,10 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     }
     __syncwarp();
   } else {
-    // ---- epilogue: warps 8 + q and 12 + q read TMEM lanes 32q..32q+31 (rows of the tile) ------
-    const int q = warp & 3, r = 32 * q + lane, eg = (warp - NSLW) >> 2;
+    // ---- epilogue: warp NSL + 4 g + q of group g reads TMEM lanes 32q..32q+31 (rows of the tile)
+    const int q = warp & 3, r = 32 * q + lane, eg = (warp - NSL) >> 2;
     const int CH = (N + 7) >> 3;        // chunks of 8 output columns per row
-    const int CHg = (CH - eg + 1) >> 1;  // chunks c = eg, eg + 2, .. of this warp per tile
+    const int CHg = (CH - eg + EG - 1) / EG;  // chunks c = eg, eg + EG, .. of this warp per tile
     const int cpb = NB >> 3;            // chunks per block (even)
     const bool need_c = !p.beta_zero;
     // the FP64-pipe finisher where the epilogue runs no beta FMA on that pipe (measured: with the
@@ -486,7 +495,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
             cp_async8(dst + 8 * x, bytes ? (const void*)(src + x) : (const void*)p.C, bytes);
           }
         }
-        pf_c += 2;
+        pf_c += EG;
         if (pf_c >= CH) {
           pf_c = eg;
           pf_it++;
@@ -497,7 +506,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     };
     if (need_c)
       for (int i = 0; i < CD - 1; i++) issue();
-    const bool issuer = p.la > 0 && warp == NSLW;
+    const bool issuer = p.la > 0 && warp == NSL;
     if (issuer)
       for (int j = 0; j < p.la && j < nt; j++) issue_tile(j);
     int g = 0;  // this warp's chunks consumed so far
@@ -527,7 +536,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
         tc_after();
         const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(k * 8 * NB);
         const int c_hi = min(CH, (cb + 1) * cpb);
-        for (int c = cb * cpb + eg; c < c_hi; c += 2, g++) {
+        // this warp's chunks of the block: c = eg (mod EG)
+        for (int c = cb * cpb + ((eg - cb * cpb) % EG + EG) % EG; c < c_hi; c += EG, g++) {
           if (need_c) issue();  // chunk g + CD - 1, into the slot of chunk g - 1, read in full already
           uint32_t raw[8][8];
 #pragma unroll
@@ -672,7 +682,9 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   a.bbytes = (uint32_t)round_up((int64_t)2 * DIGITS * MP * a.NM, 1024);
   const int HDR = MP == 64 ? hdr_bytes<64>() : (MP == 32 ? hdr_bytes<32>() : hdr_bytes<16>());
   const int64_t cbytes =
-      (int64_t)2 * (MP == 64 ? c_depth<64>() : (MP == 32 ? c_depth<32>() : c_depth<16>())) * CHUNK_BYTES;
+      (int64_t)(MP == 64 ? epi_groups<64>() * c_depth<64>()
+                         : (MP == 32 ? epi_groups<32>() * c_depth<32>() : epi_groups<16>() * c_depth<16>())) *
+      CHUNK_BYTES;
   // the deepest A' ring that fits beside B' and the old-C rings (one stage at MP = 64)
   a.nast = 0;
   for (int ns = MAXAST; ns >= 1 && a.nast == 0; ns--)
