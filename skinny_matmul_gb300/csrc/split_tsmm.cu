@@ -118,6 +118,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
@@ -221,8 +226,8 @@ __device__ __forceinline__ int f32_int23_near(float f) { return 2 * (__float_as_
 // The double W * 2^(er + fc - 2100) then comes from one of two finishers (same accuracy): the
 // integer one runs on the ALU pipe, the conversion one on the FP64 pipe, which is free for it
 // when the epilogue has no beta FMA.  W == 0 and results below the normal range give 0.
-template <int MP>
-__device__ __forceinline__ long long level_window(const uint32_t (&raw)[8][8], int x) {
+template <int MP, int W>
+__device__ __forceinline__ long long level_window(const uint32_t (&raw)[8][W], int x) {
   int d[8];
 #pragma unroll
   for (int L = 0; L < 8; L++) {
@@ -539,57 +544,59 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
         // this warp's chunks of the block: c = eg (mod EG)
         for (int c = cb * cpb + ((eg - cb * cpb) % EG + EG) % EG; c < c_hi; c += EG, g++) {
           if (need_c) issue();  // chunk g + CD - 1, into the slot of chunk g - 1, read in full already
-          uint32_t raw[8][8];
+          // the chunk in two halves of 4 columns: half the TMEM values live at a time, so that the
+          // conversion chains of a half fit the registers side by side
+          const double2* cs = reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + g % CD) * CHUNK_BYTES + r * 64);
+          if (need_c) cp_async_wait<CD - 1>();  // this thread's copies of chunk g have landed
 #pragma unroll
-          for (int L = 0; L < 8; L++) tmem_ld8(tb + (uint32_t)(L * NB + 8 * (c - cb * cpb)), raw[L]);
-          double cold[8];
-          if (need_c) {
-            cp_async_wait<CD - 1>();  // this thread's copies of chunk g have landed
-            const double2* cs =
-                reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + g % CD) * CHUNK_BYTES + r * 64);
+          for (int hh = 0; hh < 2; hh++) {
+            uint32_t raw[8][4];
 #pragma unroll
-            for (int x = 0; x < 4; x++) {
-              const double2 w = cs[x];
-              cold[2 * x] = w.x;
-              cold[2 * x + 1] = w.y;
-            }
-          }
-          tmem_wait();
-          if (live) {
-            // all eight columns are formed (columns beyond N hold zero digits and exponent 0) and
-            // masked only at the store
-            const int c0 = 8 * c;
-            const int4 f0 = *reinterpret_cast<const int4*>(fcol + c0), f1 = *reinterpret_cast<const int4*>(fcol + c0 + 4);
-            const int fc[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
-            double out[8];
-            if (cvt) {
-#pragma unroll
-              for (int x = 0; x < 8; x++) out[x] = window_cvt(level_window<MP>(raw, x), e + fc[x] - 1086);
-            } else {
-#pragma unroll
-              for (int x = 0; x < 8; x++) out[x] = window_int(level_window<MP>(raw, x), e + fc[x]);
-            }
+            for (int L = 0; L < 8; L++) tmem_ld4(tb + (uint32_t)(L * NB + 8 * (c - cb * cpb) + 4 * hh), raw[L]);
+            double cold[4];
             if (need_c) {
-              if (!p.cplx || p.beta[1] == 0.0) {  // a real beta scales both parts of a complex C alike
+              const double2 w0 = cs[2 * hh], w1 = cs[2 * hh + 1];
+              cold[0] = w0.x;
+              cold[1] = w0.y;
+              cold[2] = w1.x;
+              cold[3] = w1.y;
+            }
+            tmem_wait();
+            if (live) {
+              // all four columns are formed (columns beyond N hold zero digits and exponent 0)
+              // and masked only at the store
+              const int c0 = 8 * c + 4 * hh;
+              const int4 f = *reinterpret_cast<const int4*>(fcol + c0);
+              const int fc[4] = {f.x, f.y, f.z, f.w};
+              double out[4];
+              if (cvt) {
 #pragma unroll
-                for (int x = 0; x < 8; x++) out[x] = fma(p.beta[0], cold[x], out[x]);
+                for (int x = 0; x < 4; x++) out[x] = window_cvt(level_window<MP>(raw, x), e + fc[x] - 1086);
               } else {
 #pragma unroll
-                for (int x = 0; x < 8; x += 2) {  // (re, im) pairs: c0 is a multiple of 8
-                  const double cr = cold[x], ci = cold[x + 1];
-                  out[x] = fma(p.beta[0], cr, fma(-p.beta[1], ci, out[x]));
-                  out[x + 1] = fma(p.beta[0], ci, fma(p.beta[1], cr, out[x + 1]));
+                for (int x = 0; x < 4; x++) out[x] = window_int(level_window<MP>(raw, x), e + fc[x]);
+              }
+              if (need_c) {
+                if (!p.cplx || p.beta[1] == 0.0) {  // a real beta scales both parts of a complex C alike
+#pragma unroll
+                  for (int x = 0; x < 4; x++) out[x] = fma(p.beta[0], cold[x], out[x]);
+                } else {
+#pragma unroll
+                  for (int x = 0; x < 4; x += 2) {  // (re, im) pairs: c0 is a multiple of 4
+                    const double cr = cold[x], ci = cold[x + 1];
+                    out[x] = fma(p.beta[0], cr, fma(-p.beta[1], ci, out[x]));
+                    out[x + 1] = fma(p.beta[0], ci, fma(p.beta[1], cr, out[x + 1]));
+                  }
                 }
               }
-            }
-            if (p.vecc && c0 + 8 <= N) {
+              if (p.vecc && c0 + 4 <= N) {
+                *reinterpret_cast<double2*>(crow + c0) = make_double2(out[0], out[1]);
+                *reinterpret_cast<double2*>(crow + c0 + 2) = make_double2(out[2], out[3]);
+              } else {
 #pragma unroll
-              for (int x = 0; x < 8; x += 2)
-                *reinterpret_cast<double2*>(crow + c0 + x) = make_double2(out[x], out[x + 1]);
-            } else {
-#pragma unroll
-              for (int x = 0; x < 8; x++)
-                if (c0 + x < N) crow[c0 + x] = out[x];
+                for (int x = 0; x < 4; x++)
+                  if (c0 + x < N) crow[c0 + x] = out[x];
+              }
             }
           }
         }
