@@ -248,6 +248,11 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_R32:
       if (acc == SKINNY_ACC_DD)  // FP64 accumulation of exact products
         return run_t<float, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+      if (acc == SKINNY_ACC_SPLIT) {  // exact products on the tensor cores (TSMM)
+        if (tsmm) return split_tsmm_t(h, false, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
+        set_error("split precision for FP32 data: TSMM only (TSMTTSM: native or dd)");
+        return SKINNY_UNSUPPORTED;
+      }
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<float, float>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
@@ -267,6 +272,11 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_C32:
       if (acc == SKINNY_ACC_DD)  // complex FP64 accumulation of exact products
         return run_t<c32, c64>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
+      if (acc == SKINNY_ACC_SPLIT) {
+        if (tsmm) return split_tsmm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
+        set_error("split precision for complex FP32 data: TSMM only (TSMTTSM: native or dd)");
+        return SKINNY_UNSUPPORTED;
+      }
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<c32, c32>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;

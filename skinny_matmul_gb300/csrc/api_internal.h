@@ -88,6 +88,11 @@ skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64
 skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64_t K, const double* A,
                          int64_t lda, const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
                          int64_t ldc, cudaStream_t st, bool autoselect);
+// The same for FP32 / complex FP32 storage as well (f32: A, B, C, alpha, beta are float): values
+// widened exactly to FP64 in registers, the result rounded once to FP32 after beta * C in FP64.
+skinny_status split_tsmm_t(skinny_handle h, bool cplx, bool f32, int64_t M, int64_t N, int64_t K, const void* A,
+                           int64_t lda, const void* alpha, const void* B, int64_t ldb, const void* beta, void* C,
+                           int64_t ldc, cudaStream_t st, bool autoselect);
 
 // Frees the grouped-launch buffers owned by a handle (group.cu).
 void group_release(skinny_handle h);

@@ -75,9 +75,9 @@ template <int MP>
 __host__ __device__ constexpr int c_depth() { return MP == 64 ? 2 : (MP == 32 ? 3 : 4); }
 
 struct Args {
-  const double* A;
-  const double* B;  // real: B[n*ldb+m]; complex: the complex B (interleaved)
-  double* C;
+  const void* A;    // storage type T of the kernel (double or float), as B and C
+  const void* B;    // real: B[n*ldb+m]; complex: the complex B (interleaved)
+  void* C;
   int64_t K, lda, ldb, ldc;  // in doubles (complex: lda, ldc already doubled; ldb in complex elements)
   int M, N;                  // real widths (complex: 2M, 2N)
   int NM;                    // output width padded: 16, 32 or 64
@@ -162,14 +162,16 @@ __device__ __forceinline__ uint32_t kmaj(int row, int koct, uint32_t lbo) {
 
 // value of (alpha * B + fold * I) at (m, n) in the real view, 0 outside M x N; fold is beta for
 // the in-place product with M == N (C = A (alpha B + beta I)), else 0
+template <typename T>
 __device__ __forceinline__ double alpha_b(const Args& p, int m, int n) {
   if (m >= p.M || n >= p.N) return 0.0;
+  const T* B = static_cast<const T*>(p.B);
   if (!p.cplx) {
-    const double v = p.B[(int64_t)n * p.ldb + m] * p.alpha[0];
+    const double v = (double)B[(int64_t)n * p.ldb + m] * p.alpha[0];
     return (p.fold && m == n) ? v + p.beta[0] : v;
   }
   const int nc = n >> 1, mc = m >> 1;
-  const double br = p.B[2 * ((int64_t)nc * p.ldb + mc)], bi = p.B[2 * ((int64_t)nc * p.ldb + mc) + 1];
+  const double br = B[2 * ((int64_t)nc * p.ldb + mc)], bi = B[2 * ((int64_t)nc * p.ldb + mc) + 1];
   double ar = br * p.alpha[0] - bi * p.alpha[1], ai = br * p.alpha[1] + bi * p.alpha[0];
   if (p.fold && mc == nc) {
     ar += p.beta[0];
@@ -178,17 +180,29 @@ __device__ __forceinline__ double alpha_b(const Args& p, int m, int n) {
   return ((n & 1) == 0) ? ((m & 1) == 0 ? ar : -ai) : ((m & 1) == 0 ? ai : ar);
 }
 
-// A row values of this thread's half of the columns (MP/2 values) for tile row r0 + row
-template <int HALF>
+// A row values of this thread's part of the columns (HALF values) for tile row r0 + row, widened
+// to double (exact for float)
+template <int HALF, typename T>
 __device__ __forceinline__ void load_row(const Args& p, int64_t r0, int row, int rows, int m0, double (&v)[HALF]) {
   const bool ok = row < rows;
-  const double* a = p.A + (r0 + row) * p.lda + m0;
+  const T* a = static_cast<const T*>(p.A) + (r0 + row) * p.lda + m0;
   if (ok && p.vec && m0 + HALF <= p.M) {
+    if constexpr (sizeof(T) == 8) {
 #pragma unroll
-    for (int j = 0; j < HALF; j += 2) {
-      double2 x = p.inplace ? *reinterpret_cast<const double2*>(a + j) : __ldg(reinterpret_cast<const double2*>(a + j));
-      v[j] = x.x;
-      v[j + 1] = x.y;
+      for (int j = 0; j < HALF; j += 2) {
+        double2 x = p.inplace ? *reinterpret_cast<const double2*>(a + j) : __ldg(reinterpret_cast<const double2*>(a + j));
+        v[j] = x.x;
+        v[j + 1] = x.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < HALF; j += 4) {
+        float4 x = p.inplace ? *reinterpret_cast<const float4*>(a + j) : __ldg(reinterpret_cast<const float4*>(a + j));
+        v[j] = x.x;
+        v[j + 1] = x.y;
+        v[j + 2] = x.z;
+        v[j + 3] = x.w;
+      }
     }
   } else {
 #pragma unroll
@@ -288,13 +302,17 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src, uint32_t s
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
                : "memory");
 }
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <int MP>
+template <int MP, typename T>
 __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
   constexpr int NSL = slicer_warps<MP>(), NEP = 16 - NSL, EG = epi_groups<MP>();
   constexpr int TPS = NSL * 32 / ROWS;  // slicer threads per row (1 or 2)
@@ -349,7 +367,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
   // ---- B' = digits of alpha * B: column exponents, then (n, m-octet) units -------------------
   if (tid < p.NM) {
     uint32_t f = 0;
-    for (int m = 0; m < M; m++) f = max(f, exp_field(alpha_b(p, m, tid)));
+    for (int m = 0; m < M; m++) f = max(f, exp_field(alpha_b<T>(p, m, tid)));
     fcol[tid] = (int)f;
   }
   __syncthreads();
@@ -358,7 +376,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     float d[8][DIGITS];
     bool ng[8];
 #pragma unroll
-    for (int q2 = 0; q2 < 8; q2++) digits_of(alpha_b(p, mo * 8 + q2, n), (uint32_t)fcol[n], d[q2], ng[q2]);
+    for (int q2 = 0; q2 < 8; q2++) digits_of(alpha_b<T>(p, mo * 8 + q2, n), (uint32_t)fcol[n], d[q2], ng[q2]);
     unsigned char* bcol = bdig + (uint32_t)(n / NB) * bcb;
 #pragma unroll
     for (int j = 0; j < DIGITS; j++) {
@@ -412,7 +430,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
     double v[PART];
     auto load_tile = [&](int it) {
       const int64_t r1 = (t_begin + it) * ROWS;
-      load_row<PART>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, v);
+      load_row<PART, T>(p, r1, row, (int)((p.K - r1) < ROWS ? (p.K - r1) : ROWS), m0, v);
     };
     if (nt > 0) load_tile(0);
     for (int it = 0; it < nt; it++) {
@@ -484,20 +502,24 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
         const int c = pf_c;
         const int64_t rr = (t_begin + pf_it) * ROWS + r;
         const bool live = rr < p.K;
-        const double* src = p.C + rr * p.ldc + 8 * c;
+        const T* src = static_cast<const T*>(p.C) + rr * p.ldc + 8 * c;
         unsigned char* dst = cbuf + (size_t)(eg * CD + pf_g % CD) * CHUNK_BYTES + r * 64;
+        constexpr int PER16 = 16 / (int)sizeof(T);  // elements per 16-byte piece
         if (p.vecc) {
 #pragma unroll
-          for (int x = 0; x < 4; x++) {
-            const int left = N - (8 * c + 2 * x);
-            const uint32_t bytes = live ? (uint32_t)(left >= 2 ? 16 : (left == 1 ? 8 : 0)) : 0u;
-            cp_async16(dst + 16 * x, bytes ? (const void*)(src + 2 * x) : (const void*)p.C, bytes);
+          for (int x = 0; x < 8 / PER16; x++) {
+            const int left = N - (8 * c + PER16 * x);
+            const uint32_t bytes = live && left > 0 ? (uint32_t)(min(left, PER16) * (int)sizeof(T)) : 0u;
+            cp_async16(dst + 16 * x, bytes ? (const void*)(src + PER16 * x) : p.C, bytes);
           }
         } else {
 #pragma unroll
           for (int x = 0; x < 8; x++) {
-            const uint32_t bytes = (live && 8 * c + x < N) ? 8u : 0u;
-            cp_async8(dst + 8 * x, bytes ? (const void*)(src + x) : (const void*)p.C, bytes);
+            const uint32_t bytes = (live && 8 * c + x < N) ? (uint32_t)sizeof(T) : 0u;
+            if constexpr (sizeof(T) == 8)
+              cp_async8(dst + 8 * x, bytes ? (const void*)(src + x) : p.C, bytes);
+            else
+              cp_async4(dst + 4 * x, bytes ? (const void*)(src + x) : p.C, bytes);
           }
         }
         pf_c += EG;
@@ -530,7 +552,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
       const int e = erow[es * ROWS + r] - 1014;
       __syncwarp();
       if (lane == 0) mbar_arrive(&eempty[es]);
-      double* crow = p.C + rr * p.ldc;
+      T* crow = static_cast<T*>(p.C) + rr * p.ldc;
       for (int cb = 0; cb < p.ncb; cb++, job++) {
         const int k = job % p.nsets;
         ok = wait_ab(&tfull[k], (uint32_t)((job / p.nsets) & 1), abort_f, p.err);
@@ -546,7 +568,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
           if (need_c) issue();  // chunk g + CD - 1, into the slot of chunk g - 1, read in full already
           // the chunk in two halves of 4 columns: half the TMEM values live at a time, so that the
           // conversion chains of a half fit the registers side by side
-          const double2* cs = reinterpret_cast<const double2*>(cbuf + (size_t)(eg * CD + g % CD) * CHUNK_BYTES + r * 64);
+          const unsigned char* cs = cbuf + (size_t)(eg * CD + g % CD) * CHUNK_BYTES + r * 64;
           if (need_c) cp_async_wait<CD - 1>();  // this thread's copies of chunk g have landed
 #pragma unroll
           for (int hh = 0; hh < 2; hh++) {
@@ -555,11 +577,20 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
             for (int L = 0; L < 8; L++) tmem_ld4(tb + (uint32_t)(L * NB + 8 * (c - cb * cpb) + 4 * hh), raw[L]);
             double cold[4];
             if (need_c) {
-              const double2 w0 = cs[2 * hh], w1 = cs[2 * hh + 1];
-              cold[0] = w0.x;
-              cold[1] = w0.y;
-              cold[2] = w1.x;
-              cold[3] = w1.y;
+              if constexpr (sizeof(T) == 8) {
+                const double2 w0 = reinterpret_cast<const double2*>(cs)[2 * hh];
+                const double2 w1 = reinterpret_cast<const double2*>(cs)[2 * hh + 1];
+                cold[0] = w0.x;
+                cold[1] = w0.y;
+                cold[2] = w1.x;
+                cold[3] = w1.y;
+              } else {
+                const float4 w = reinterpret_cast<const float4*>(cs)[hh];
+                cold[0] = w.x;
+                cold[1] = w.y;
+                cold[2] = w.z;
+                cold[3] = w.w;
+              }
             }
             tmem_wait();
             if (live) {
@@ -590,12 +621,16 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
                 }
               }
               if (p.vecc && c0 + 4 <= N) {
-                *reinterpret_cast<double2*>(crow + c0) = make_double2(out[0], out[1]);
-                *reinterpret_cast<double2*>(crow + c0 + 2) = make_double2(out[2], out[3]);
+                if constexpr (sizeof(T) == 8) {
+                  *reinterpret_cast<double2*>(crow + c0) = make_double2(out[0], out[1]);
+                  *reinterpret_cast<double2*>(crow + c0 + 2) = make_double2(out[2], out[3]);
+                } else {  // the one rounding of an FP32 result
+                  *reinterpret_cast<float4*>(crow + c0) = make_float4((float)out[0], (float)out[1], (float)out[2], (float)out[3]);
+                }
               } else {
 #pragma unroll
                 for (int x = 0; x < 4; x++)
-                  if (c0 + x < N) crow[c0 + x] = out[x];
+                  if (c0 + x < N) crow[c0 + x] = (T)out[x];
               }
             }
           }
@@ -618,11 +653,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmm_kernel(const Args p) {
 
 }  // namespace stsmm
 
-skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64_t K, const double* A,
-                         int64_t lda, const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
-                         int64_t ldc, cudaStream_t st, bool autoselect) {
+skinny_status split_tsmm_t(skinny_handle h, bool cplx, bool f32, int64_t M, int64_t N, int64_t K, const void* A,
+                           int64_t lda, const void* alpha, const void* B, int64_t ldb, const void* beta, void* C,
+                           int64_t ldc, cudaStream_t st, bool autoselect) {
   using namespace stsmm;
   const int64_t Mr = cplx ? 2 * M : M, Nr = cplx ? 2 * N : N;
+  const int64_t es = f32 ? 4 : 8;  // bytes of a real storage element
   if (Mr > 64 || Nr > 64) {
     // wider products out of place run as passes of real width <= 64: output columns are
     // independent, and the contraction accumulates through beta (the first pass applies beta,
@@ -637,11 +673,15 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
       return SKINNY_UNSUPPORTED;
     }
     const double one[2] = {1.0, 0.0};
+    const float onef[2] = {1.0f, 0.0f};
+    const char *a8 = static_cast<const char*>(A), *b8 = static_cast<const char*>(B);
+    char* c8 = static_cast<char*>(C);
     for (int64_t n0 = 0; n0 < N; n0 += cw)
       for (int64_t m0 = 0; m0 < M; m0 += cw) {
-        const skinny_status s = split_tsmm(h, cplx, std::min(cw, M - m0), std::min(cw, N - n0), K, A + w * m0, lda,
-                                           alpha, B + w * (n0 * ldb + m0), ldb, m0 == 0 ? beta : (const void*)one,
-                                           C + w * n0, ldc, st, false);
+        const skinny_status s = split_tsmm_t(
+            h, cplx, f32, std::min(cw, M - m0), std::min(cw, N - n0), K, a8 + w * m0 * es, lda, alpha,
+            b8 + w * (n0 * ldb + m0) * es, ldb, m0 == 0 ? beta : (f32 ? (const void*)onef : (const void*)one),
+            c8 + w * n0 * es, ldc, st, false);
         if (s != SKINNY_OK) return s;
       }
     return SKINNY_OK;
@@ -673,15 +713,22 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   a.cplx = cplx;
   std::memset(a.alpha, 0, sizeof a.alpha);
   std::memset(a.beta, 0, sizeof a.beta);
-  std::memcpy(a.alpha, alpha, cplx ? 16 : 8);
-  std::memcpy(a.beta, beta, cplx ? 16 : 8);
+  if (f32) {  // FP32 scalars widened (exactly)
+    float af[2] = {0.0f, 0.0f}, bf[2] = {0.0f, 0.0f};
+    std::memcpy(af, alpha, cplx ? 8 : 4);
+    std::memcpy(bf, beta, cplx ? 8 : 4);
+    a.alpha[0] = af[0], a.alpha[1] = af[1], a.beta[0] = bf[0], a.beta[1] = bf[1];
+  } else {
+    std::memcpy(a.alpha, alpha, cplx ? 16 : 8);
+    std::memcpy(a.beta, beta, cplx ? 16 : 8);
+  }
   a.beta_zero = a.beta[0] == 0.0 && a.beta[1] == 0.0;
   a.inplace = (const void*)A == (const void*)C;
   // in place with M == N: C = A (alpha B + beta I); the epilogue then needs no old C and no FMA
   a.fold = a.inplace && M == N && !a.beta_zero;
   if (a.fold) a.beta_zero = 1;
-  a.vec = ((uintptr_t)A % 16 == 0) && (a.lda % 2 == 0);
-  a.vecc = ((uintptr_t)C % 16 == 0) && (a.ldc % 2 == 0);
+  a.vec = ((uintptr_t)A % 16 == 0) && ((a.lda * es) % 16 == 0);
+  a.vecc = ((uintptr_t)C % 16 == 0) && ((a.ldc * es) % 16 == 0);
   a.NB = a.NM == 16 ? 16 : 32;
   a.ncb = a.NM / a.NB;
   a.nsets = 512 / (8 * a.NB);
@@ -709,21 +756,21 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
   const int smem = (int)(HDR + (int64_t)a.bbytes + (int64_t)a.nast * a.astage + cbytes);
   int64_t grid = std::min<int64_t>((int64_t)h->dev.sms, a.ntiles);
   if (grid < 1) grid = 1;
-  static SmemAttr attr16, attr32, attr64;
+  static SmemAttr attr[6];
+  auto launch = [&](auto kern, SmemAttr& at) {
+    const bool ok = ensure_smem_attr(kern, smem, at);
+    if (ok) kern<<<(int)grid, THREADS, smem, st>>>(a);
+    return ok;
+  };
   bool attr_ok;
-  switch (MP) {
-    case 16:
-      attr_ok = ensure_smem_attr(split_tsmm_kernel<16>, smem, attr16);
-      if (attr_ok) split_tsmm_kernel<16><<<(int)grid, THREADS, smem, st>>>(a);
-      break;
-    case 32:
-      attr_ok = ensure_smem_attr(split_tsmm_kernel<32>, smem, attr32);
-      if (attr_ok) split_tsmm_kernel<32><<<(int)grid, THREADS, smem, st>>>(a);
-      break;
-    default:
-      attr_ok = ensure_smem_attr(split_tsmm_kernel<64>, smem, attr64);
-      if (attr_ok) split_tsmm_kernel<64><<<(int)grid, THREADS, smem, st>>>(a);
-      break;
+  if (!f32) {
+    attr_ok = MP == 16 ? launch(split_tsmm_kernel<16, double>, attr[0])
+              : MP == 32 ? launch(split_tsmm_kernel<32, double>, attr[1])
+                         : launch(split_tsmm_kernel<64, double>, attr[2]);
+  } else {
+    attr_ok = MP == 16 ? launch(split_tsmm_kernel<16, float>, attr[3])
+              : MP == 32 ? launch(split_tsmm_kernel<32, float>, attr[4])
+                         : launch(split_tsmm_kernel<64, float>, attr[5]);
   }
   if (!attr_ok) return SKINNY_DEVICE_ERROR;  // the error text is set
   count_launch();
@@ -733,6 +780,12 @@ skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64
     return SKINNY_DEVICE_ERROR;
   }
   return SKINNY_OK;
+}
+
+skinny_status split_tsmm(skinny_handle h, bool cplx, int64_t M, int64_t N, int64_t K, const double* A,
+                         int64_t lda, const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
+                         int64_t ldc, cudaStream_t st, bool autoselect) {
+  return split_tsmm_t(h, cplx, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, autoselect);
 }
 
 }  // namespace skinny

@@ -25,13 +25,17 @@ CASES = [c for c in common.int_cases() if c["op"] == "tsmm" and
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: c["id"])
-def test_split_tsmm_golden_bit_exact(handle, case):
+@pytest.mark.parametrize("single", [False, True], ids=["fp64", "fp32"])
+def test_split_tsmm_golden_bit_exact(handle, case, single):
+    """The integer fixtures, in FP64 / complex FP64 and in FP32 / complex FP32 storage (their
+    values and results are exact in both)."""
     c = case
-    A, B, C = dev(c["A"]), dev(c["B"]), dev(c["C"])
+    dt = (np.complex64 if c["cplx"] else np.float32) if single else (np.complex128 if c["cplx"] else np.float64)
+    A, B, C = dev(c["A"].astype(dt)), dev(c["B"].astype(dt)), dev(c["C"].astype(dt))
     if c["self"]:
         A = C
     handle.tsmm(c["M"], c["N"], c["K"], A, c["lda"], 1.0, B, c["ldb"], float(c["beta"]), C, c["ldc"], acc="split")
-    got = host(C)
+    got = host(C).astype(np.complex128 if c["cplx"] else np.float64)
     assert np.array_equal(got, c["exp"])
 
 
@@ -81,6 +85,37 @@ def test_split_tsmm_complex(handle, M, N, inplace):
     exp, den = common.tsmm_expected(M, N, K, C0 if inplace else A, lda, B, ldb, C0, ldc, alpha, beta)
     err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
     assert err <= min(common.tol(np.complex128, M), 8e-16), err
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex64])
+@pytest.mark.parametrize("M,N", [(1, 1), (4, 4), (8, 8), (16, 16), (4, 16), (8, 32), (3, 7), (32, 32), (64, 64),
+                                 (17, 9), (40, 8)])
+@pytest.mark.parametrize("inplace", [False, True])
+def test_split_tsmm_fp32(handle, dt, M, N, inplace):
+    """FP32 and complex FP32 storage on the split kernel: exact products, FP64-accurate sums, one
+    rounding to FP32 at the end -- within 2^-23 normwise of the exact result (the native FP32
+    kernels are held to 8 sqrt(M) 2^-24); odd leading dimensions take the unvectorised paths."""
+    if inplace and M != N:
+        pytest.skip("in place needs M == N here")
+    cplx = dt == np.complex64
+    if cplx and max(M, N) > 32:
+        M, N = min(M, 32), min(N, 32)
+    rng = np.random.default_rng(11 + M * 7 + N)
+    K = 9001
+    lda, ldb, ldc = (M, M + 1, N) if not inplace else (M, M, M)
+    if M == 3:
+        lda, ldc = M + 2, N + 1  # 4-byte rows that are not 16-byte multiples
+    A = common.uniform(rng, K * lda, dt)
+    B = common.uniform(rng, N * ldb, dt)
+    C0 = A.copy() if inplace else common.uniform(rng, K * ldc, dt)
+    alpha, beta = (1.0 + 0.5j, 0.5 - 0.25j) if cplx else (1.5, -0.5)
+    Cd = dev(C0)
+    Ad = Cd if inplace else dev(A)
+    handle.tsmm(M, N, K, Ad, lda, alpha, dev(B), ldb, beta, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmm_expected(M, N, K, C0 if inplace else A, lda, B, ldb, C0, ldc, alpha, beta)
+    err = common.normwise(got, exp, den, common.c_mask_tsmm(N, K, ldc))
+    assert err <= 2.0 ** -23, err
 
 
 def test_split_tsmm_wide_exponents_and_zero_rows(handle):
