@@ -248,11 +248,9 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_R32:
       if (acc == SKINNY_ACC_DD)  // FP64 accumulation of exact products
         return run_t<float, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
-      if (acc == SKINNY_ACC_SPLIT) {  // exact products on the tensor cores (TSMM)
-        if (tsmm) return split_tsmm_t(h, false, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
-        set_error("split precision for FP32 data: TSMM only (TSMTTSM: native or dd)");
-        return SKINNY_UNSUPPORTED;
-      }
+      if (acc == SKINNY_ACC_SPLIT)  // exact products on the tensor cores (TSMTTSM: M, N <= 16)
+        return tsmm ? split_tsmm_t(h, false, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false)
+                    : split_tsmttsm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<float, float>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
@@ -272,11 +270,9 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_C32:
       if (acc == SKINNY_ACC_DD)  // complex FP64 accumulation of exact products
         return run_t<c32, c64>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
-      if (acc == SKINNY_ACC_SPLIT) {
-        if (tsmm) return split_tsmm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
-        set_error("split precision for complex FP32 data: TSMM only (TSMTTSM: native or dd)");
-        return SKINNY_UNSUPPORTED;
-      }
+      if (acc == SKINNY_ACC_SPLIT)  // (TSMTTSM: M, N <= 8)
+        return tsmm ? split_tsmm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false)
+                    : split_complex_tsmttsm(h, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false, false, true);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
         return run_t<c32, c32>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
       break;
@@ -288,7 +284,7 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
         skinny_status s =
             tsmm ? split_tsmm(h, true, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
                               (double*)C, ldc, st, autosel)
-                 : split_complex_tsmttsm(h, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+                 : split_complex_tsmttsm(h, M, N, K, A, lda, alpha, B, ldb, beta,
                                          (double*)C, ldc, st, autosel);
         if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
       }
@@ -342,7 +338,7 @@ skinny_status dispatch_conj(skinny_handle h, skinny_dtype dt, skinny_acc acc, in
                             const void* beta, void* C, int64_t ldc, cudaStream_t st) {
   LaunchOpts o{};
   if (dt == SKINNY_C64 && (acc == SKINNY_ACC_SPLIT || acc == SKINNY_ACC_AUTO)) {
-    skinny_status s = split_complex_tsmttsm(h, M, N, K, (const double*)A, lda, alpha, (const double*)B, ldb, beta,
+    skinny_status s = split_complex_tsmttsm(h, M, N, K, A, lda, alpha, B, ldb, beta,
                                             (double*)C, ldc, st, acc == SKINNY_ACC_AUTO, true);
     if (s != SKINNY_UNSUPPORTED || acc == SKINNY_ACC_SPLIT) return s;
   }

@@ -68,9 +68,9 @@ constexpr uint32_t SLEEP_PRODUCER = 64;  // ns between polls of the producer war
 constexpr uint32_t SLEEP_MMA = 32;       // ns between polls of the MMA thread
 
 struct Args {
-  const double* A;
-  const double* B;
-  double* C;
+  const void* A;  // FP64, or FP32 with in_f32 (widened exactly when read)
+  const void* B;
+  void* C;        // FP64, or FP32 with out_f32
   int64_t K, lda, ldb, ldc;
   int M, N, MP, NP;  // padded widths (powers of two); NP = MP in Gram mode
   double alpha, beta;
@@ -87,6 +87,7 @@ struct Args {
   double* partials;
   unsigned* counter;
   int* err;
+  int out_f32;
 };
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo) {
@@ -208,7 +209,7 @@ __device__ __forceinline__ bool wait_ab(uint64_t* bar, uint32_t parity, volatile
   return false;
 }
 
-template <int NP>
+template <int NP, typename TI>
 __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p) {
   constexpr int BN = NP < 8 ? NP : 8;  // B columns per drain block
   constexpr int NB = NP / BN;          // drain blocks
@@ -293,11 +294,12 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
         const int64_t tt = t_begin + t;
         if (is_bulk(tt)) {
           const int64_t r0 = tt * p.rr;
-          const uint32_t ba = (uint32_t)(p.rr * p.lda * 8), bb = p.gram ? 0u : (uint32_t)(p.rr * p.ldb * 8);
+          constexpr uint32_t ES = sizeof(TI);
+          const uint32_t ba = (uint32_t)(p.rr * p.lda * ES), bb = p.gram ? 0u : (uint32_t)(p.rr * p.ldb * ES);
           unsigned char* st = ring + (size_t)s * p.stage_bytes;
           mbar_arrive_expect_tx(&full[s], ba + bb);
-          bulk_g2s(st, p.A + r0 * p.lda, ba, &full[s]);
-          if (!p.gram) bulk_g2s(st + p.tile_a, p.B + r0 * p.ldb, bb, &full[s]);
+          bulk_g2s(st, static_cast<const TI*>(p.A) + r0 * p.lda, ba, &full[s]);
+          if (!p.gram) bulk_g2s(st + p.tile_a, static_cast<const TI*>(p.B) + r0 * p.ldb, bb, &full[s]);
         } else {
           mbar_arrive(&full[s]);  // no copy: the slicers read this round from global memory
         }
@@ -467,8 +469,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
       const int rows = (int)((p.K - r0) < p.rr ? (p.K - r0) : p.rr);
       const bool ok = wait_ab(&full[s], (uint32_t)((t / p.stages) & 1), abort_f, p.err);
       const bool blk = is_bulk(tt);
-      const double* stA = reinterpret_cast<const double*>(ring + (size_t)s * p.stage_bytes);
-      const double* stB = p.gram ? stA : reinterpret_cast<const double*>(ring + (size_t)s * p.stage_bytes + p.tile_a);
+      const TI* stA = reinterpret_cast<const TI*>(ring + (size_t)s * p.stage_bytes);
+      const TI* stB = p.gram ? stA : reinterpret_cast<const TI*>(ring + (size_t)s * p.stage_bytes + p.tile_a);
       double v[2][8];
       uint32_t eu[2] = {0u, 0u};
       bool exceed = false;
@@ -481,18 +483,18 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
         const int64_t ld = isB ? p.ldb : p.lda;
         const int g = uoct[k] & 7;
         if (blk) {  // shared-memory stage
-          const double* src = isB ? stB : stA;
+          const TI* src = isB ? stB : stA;
 #pragma unroll
           for (int q2 = 0; q2 < 8; q2++) {
             const int rr = uoct[k] * 8 + (q2 ^ g);
-            v[k][q2] = (ok && uval[k]) ? src[rr * ld + ucol[k]] : 0.0;
+            v[k][q2] = (ok && uval[k]) ? (double)src[rr * ld + ucol[k]] : 0.0;
           }
         } else {  // global memory (rows not 16-byte aligned, or the last round)
-          const double* src = (isB ? p.B : p.A) + r0 * ld;
+          const TI* src = static_cast<const TI*>(isB ? p.B : p.A) + r0 * ld;
 #pragma unroll
           for (int q2 = 0; q2 < 8; q2++) {
             const int rr = uoct[k] * 8 + (q2 ^ g);
-            v[k][q2] = (ok && uval[k] && rr < rows) ? src[rr * ld + ucol[k]] : 0.0;
+            v[k][q2] = (ok && uval[k] && rr < rows) ? (double)src[rr * ld + ucol[k]] : 0.0;
           }
         }
         // largest exponent field of the unit (1 if only subnormals, 0 if all zero): the largest
@@ -582,16 +584,22 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
     double sum = red[tid];
     for (int q2 = 1; q2 < P; q2++) sum += red[q2 * MN + tid];
     const int mm = tid % M, nn = tid / M;
-    double* c = p.C + (int64_t)nn * p.ldc + mm;
-    *c = p.beta_zero ? p.alpha * sum : (*c) * p.beta + sum * p.alpha;
+    const int64_t ci = (int64_t)nn * p.ldc + mm;
+    if (p.out_f32) {  // the one rounding of an FP32 result
+      float* c = static_cast<float*>(p.C) + ci;
+      *c = (float)(p.beta_zero ? p.alpha * sum : (double)(*c) * p.beta + sum * p.alpha);
+    } else {
+      double* c = static_cast<double*>(p.C) + ci;
+      *c = p.beta_zero ? p.alpha * sum : (*c) * p.beta + sum * p.alpha;
+    }
   }
   if (tid == 0) *p.counter = 0u;
 }
 
-template <int NP>
+template <int NP, typename TI>
 static skinny_status launch(const Args& a, int grid, int smem, cudaStream_t st) {
   static SmemAttr attr;
-  auto kern = split_tsmttsm_kernel<NP>;
+  auto kern = split_tsmttsm_kernel<NP, TI>;
   ensure_smem_attr(kern, smem, attr);
   kern<<<grid, THREADS, smem, st>>>(a);
   count_launch();
@@ -609,8 +617,15 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
                             const double* A, int64_t lda, const void* alpha, const double* B,
                             int64_t ldb, const void* beta, double* C, int64_t ldc,
                             cudaStream_t st, bool autoselect) {
-  using namespace split;
   if (tsmm) return split_tsmm(h, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, autoselect);
+  return split_tsmttsm_t(h, false, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, autoselect);
+}
+
+skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M, int64_t N, int64_t K,
+                              const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                              const void* beta, void* C, int64_t ldc, cudaStream_t st, bool autoselect) {
+  using namespace split;
+  const int64_t es = in_f32 ? 4 : 8;
   if (M > 128 || N > 128) {
     set_error("split precision TSMTTSM: M, N <= 128");
     return SKINNY_UNSUPPORTED;
@@ -632,7 +647,14 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
     return SKINNY_UNSUPPORTED;
   }
   // M or N > 16: the wide kernel (64 x 64 blocks, FP16 digit planes, level accumulators)
-  if (wide) return split_wide(h, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st);
+  if (wide) {
+    if (in_f32 || out_f32) {
+      set_error("split precision TSMTTSM for FP32 data: M, N <= 16 (complex: 8)");
+      return SKINNY_UNSUPPORTED;
+    }
+    return split_wide(h, M, N, K, static_cast<const double*>(A), lda, alpha, static_cast<const double*>(B), ldb, beta,
+                      static_cast<double*>(C), ldc, st);
+  }
   Args a;
   a.A = A;
   a.B = B;
@@ -643,8 +665,17 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.ldc = ldc;
   a.M = (int)M;
   a.N = (int)N;
-  std::memcpy(&a.alpha, alpha, 8);
-  std::memcpy(&a.beta, beta, 8);
+  if (out_f32) {  // FP32 scalars widened (exactly)
+    float af, bf;
+    std::memcpy(&af, alpha, 4);
+    std::memcpy(&bf, beta, 4);
+    a.alpha = af;
+    a.beta = bf;
+  } else {
+    std::memcpy(&a.alpha, alpha, 8);
+    std::memcpy(&a.beta, beta, 8);
+  }
+  a.out_f32 = out_f32;
   a.beta_zero = a.beta == 0.0;
   a.gram = (A == B) && (lda == ldb) && (M == N);
   const int NP = pow2ceil(a.gram ? M : N);
@@ -672,8 +703,8 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
     const int64_t octs = a.rr / 8;
     a.dig_a = (uint32_t)round_up(octs * a.lbo_a + DPAD, 1024);
     a.dig_b = a.gram ? 0u : (uint32_t)round_up(octs * a.lbo_b, 1024);
-    a.tile_a = (uint32_t)round_up((int64_t)a.rr * lda * 8, 128);
-    const int64_t tile_b = a.gram ? 0 : round_up((int64_t)a.rr * ldb * 8, 128);
+    a.tile_a = (uint32_t)round_up((int64_t)a.rr * lda * es, 128);
+    const int64_t tile_b = a.gram ? 0 : round_up((int64_t)a.rr * ldb * es, 128);
     dstage = (int64_t)a.dig_a + a.dig_b;
     for (int bulk = (aligned && dense && K > a.rr) ? 1 : 0; bulk >= 0 && a.stages == 0; bulk--) {
       a.bulk = bulk;
@@ -701,12 +732,22 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;
   a.err = h->err;
-  switch (NP) {
-    case 1: return launch<1>(a, (int)grid, smem2, st);
-    case 2: return launch<2>(a, (int)grid, smem2, st);
-    case 4: return launch<4>(a, (int)grid, smem2, st);
-    case 8: return launch<8>(a, (int)grid, smem2, st);
-    case 16: return launch<16>(a, (int)grid, smem2, st);
+  if (!in_f32) {
+    switch (NP) {
+      case 1: return launch<1, double>(a, (int)grid, smem2, st);
+      case 2: return launch<2, double>(a, (int)grid, smem2, st);
+      case 4: return launch<4, double>(a, (int)grid, smem2, st);
+      case 8: return launch<8, double>(a, (int)grid, smem2, st);
+      case 16: return launch<16, double>(a, (int)grid, smem2, st);
+    }
+  } else {
+    switch (NP) {
+      case 1: return launch<1, float>(a, (int)grid, smem2, st);
+      case 2: return launch<2, float>(a, (int)grid, smem2, st);
+      case 4: return launch<4, float>(a, (int)grid, smem2, st);
+      case 8: return launch<8, float>(a, (int)grid, smem2, st);
+      case 16: return launch<16, float>(a, (int)grid, smem2, st);
+    }
   }
   set_error("split precision: unsupported N");
   return SKINNY_UNSUPPORTED;

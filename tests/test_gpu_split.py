@@ -36,6 +36,54 @@ def test_split_golden_integer_cases_bit_exact(handle, case):
     assert np.array_equal(host(C), c["exp"])
 
 
+FP32_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and c["M"] <= (8 if c["cplx"] else 16) and
+              c["N"] <= (8 if c["cplx"] else 16)]
+
+
+@pytest.mark.parametrize("case", FP32_CASES, ids=lambda c: c["id"])
+def test_split_fp32_golden_integer_cases_bit_exact(handle, case):
+    """The integer fixtures in FP32 / complex FP32 storage (exact in both) on the split kernel."""
+    c = case
+    dt = np.complex64 if c["cplx"] else np.float32
+    A, B, C = dev(c["A"].astype(dt)), dev(c["B"].astype(dt)), dev(c["C"].astype(dt))
+    if c["self"]:
+        B = A
+    handle.tsmttsm(c["M"], c["N"], c["K"], A, c["lda"], 1.0, B, c["ldb"], float(c["beta"]), C, c["ldc"], acc="split")
+    assert np.array_equal(host(C).astype(np.complex128 if c["cplx"] else np.float64), c["exp"])
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex64])
+@pytest.mark.parametrize("M,N,K", [(1, 1, 1000), (4, 4, 33333), (8, 8, 1 << 18), (16, 16, 50000), (3, 7, 4097),
+                                   (8, 2, 129)])
+def test_split_fp32_vs_exact(handle, dt, M, N, K):
+    """FP32 / complex FP32 storage on the split kernel (exact products, FP64-accurate sums, one
+    rounding to FP32): within 2^-23 normwise of the exact result, where FP32 accumulation is held
+    to 8 sqrt(K) 2^-24.  Complex widths up to 8 (their real product is 16 wide)."""
+    cplx = dt == np.complex64
+    if cplx and max(M, N) > 8:
+        pytest.skip("complex FP32 split TSMTTSM: M, N <= 8")
+    rng = np.random.default_rng(M * 31 + N * 7 + K + 5)
+    lda, ldb, ldc = M, N, M + 2
+    A = common.uniform(rng, K * lda, dt)
+    B = common.uniform(rng, K * ldb, dt)
+    C0 = common.uniform(rng, N * ldc, dt)
+    alpha, beta = (1.25 + 0.5j, -0.5 + 0.25j) if cplx else (1.25, -0.5)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), lda, alpha, dev(B), ldb, beta, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, N, K, A, lda, B, ldb, C0, ldc, alpha, beta)
+    err = common.normwise(got, exp, den, common.c_mask_tsmttsm(M, N, ldc))
+    assert err <= 2.0 ** -23, err
+
+
+def test_split_fp32_wide_is_refused(handle):
+    from skinny_matmul_gb300 import SkinnyError
+    X = dev(np.zeros(64 * 64, np.float32))
+    C = dev(np.zeros(32 * 32, np.float32))
+    with pytest.raises(SkinnyError, match="UNSUPPORTED"):
+        handle.tsmttsm(32, 32, 64, X, 32, 1.0, X[1:], 32, 0.0, C, 32, acc="split")
+
+
 SHAPES = [(1, 1, 1000), (2, 2, 70000), (4, 4, 33333), (8, 8, 1 << 20), (16, 16, 100000), (4, 16, 12345),
           (16, 4, 12345), (5, 3, 1001), (13, 7, 4096), (8, 8, 127), (8, 8, 129), (3, 3, 1)]
 
