@@ -62,9 +62,9 @@ typedef enum {
                             types.hpp:49-57), C64 double-double real and imaginary parts, R32 / C32 in
                             FP64 / complex FP64; not for the conjugate product */
   SKINNY_ACC_SPLIT = 2,  /* split precision: values sliced into FP16 digits, products on tcgen05
-                            tensor cores with exact FP32 accumulation, recombined in FP64.  R64, C64;
-                            R32 / C32 storage (widened exactly, rounded once to FP32) for TSMM and for
-                            TSMTTSM with M, N <= 16 (C32: 8).  No counterpart in the reference. */
+                            tensor cores with exact FP32 accumulation, recombined in FP64.  R64, C64,
+                            and R32 / C32 storage (widened exactly, rounded once to FP32) at the same
+                            widths.  No counterpart in the reference. */
   SKINNY_ACC_AUTO = 3    /* fastest method meeting the working precision's error bound */
 } skinny_acc;
 

@@ -248,7 +248,7 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_R32:
       if (acc == SKINNY_ACC_DD)  // FP64 accumulation of exact products
         return run_t<float, double>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
-      if (acc == SKINNY_ACC_SPLIT)  // exact products on the tensor cores (TSMTTSM: M, N <= 16)
+      if (acc == SKINNY_ACC_SPLIT)  // exact products on the tensor cores
         return tsmm ? split_tsmm_t(h, false, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false)
                     : split_tsmttsm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)
@@ -270,7 +270,7 @@ skinny_status dispatch_product(skinny_handle h, bool tsmm, skinny_dtype dt, skin
     case SKINNY_C32:
       if (acc == SKINNY_ACC_DD)  // complex FP64 accumulation of exact products
         return run_t<c32, c64>(h, tsmm, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, o);
-      if (acc == SKINNY_ACC_SPLIT)  // (TSMTTSM: M, N <= 8)
+      if (acc == SKINNY_ACC_SPLIT)
         return tsmm ? split_tsmm_t(h, true, true, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false)
                     : split_complex_tsmttsm(h, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st, false, false, true);
       if (acc == SKINNY_ACC_NATIVE || acc == SKINNY_ACC_AUTO)

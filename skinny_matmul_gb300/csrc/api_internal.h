@@ -73,7 +73,7 @@ skinny_status split_product(skinny_handle h, bool tsmm, int64_t M, int64_t N, in
                             cudaStream_t st, bool autoselect);
 
 // TSMTTSM in split precision with FP32 storage as well (split.cu): in_f32 reads A and B as FP32
-// (widened exactly), out_f32 writes C (and takes alpha, beta) as FP32; FP32 for M, N <= 16.
+// (widened exactly), out_f32 writes C (and takes alpha, beta) as FP32; M, N <= 128.
 skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M, int64_t N, int64_t K,
                               const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
                               const void* beta, void* C, int64_t ldc, cudaStream_t st, bool autoselect);
@@ -82,9 +82,13 @@ skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_
 skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
                          const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
                          int64_t ldc, cudaStream_t st);
+// The same with FP32 inputs (in_f32) and / or FP32 output, alpha and beta (out_f32).
+skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M, int64_t N, int64_t K,
+                           const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                           const void* beta, void* C, int64_t ldc, cudaStream_t st);
 
 // Complex FP64 TSMTTSM in split precision through the real product of doubled width
-// (split_complex.cu); M, N <= 64.  f32: complex FP32 storage (A, B, C, alpha, beta), M, N <= 8.
+// (split_complex.cu); M, N <= 64.  f32: complex FP32 storage (A, B, C, alpha, beta).
 skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64_t K, const void* A,
                                     int64_t lda, const void* alpha, const void* B, int64_t ldb,
                                     const void* beta, void* C, int64_t ldc, cudaStream_t st, bool autoselect,

@@ -647,14 +647,7 @@ skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_
     return SKINNY_UNSUPPORTED;
   }
   // M or N > 16: the wide kernel (64 x 64 blocks, FP16 digit planes, level accumulators)
-  if (wide) {
-    if (in_f32 || out_f32) {
-      set_error("split precision TSMTTSM for FP32 data: M, N <= 16 (complex: 8)");
-      return SKINNY_UNSUPPORTED;
-    }
-    return split_wide(h, M, N, K, static_cast<const double*>(A), lda, alpha, static_cast<const double*>(B), ldb, beta,
-                      static_cast<double*>(C), ldc, st);
-  }
+  if (wide) return split_wide_t(h, in_f32, out_f32, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st);
   Args a;
   a.A = A;
   a.B = B;

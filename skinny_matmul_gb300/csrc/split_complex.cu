@@ -49,10 +49,6 @@ skinny_status split_complex_tsmttsm(skinny_handle h, int64_t M, int64_t N, int64
     set_error("split precision complex TSMTTSM: M, N <= 64");
     return SKINNY_UNSUPPORTED;
   }
-  if (f32 && (M > 8 || N > 8)) {
-    set_error("split precision complex FP32 TSMTTSM: M, N <= 8");
-    return SKINNY_UNSUPPORTED;
-  }
   void*& buf = h->split_ws[st];  // P, at most 128 x 128 doubles, one per stream
   if (!buf) {
     if (cudaMalloc(&buf, (size_t)4 * CMAX * CMAX * sizeof(double)) != cudaSuccess) {

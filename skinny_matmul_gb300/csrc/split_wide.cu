@@ -74,9 +74,9 @@ constexpr int MAX_EPOCH_PERIODS = 1 << 14;     // int64 words hold 2^15 periods 
 constexpr int GROUP = 16;                      // chunks per first-level group of the finish (<= 15 groups)
 
 struct Args {
-  const double* A;
-  const double* B;
-  double* C;
+  const void* A;  // FP64, or FP32 (widened exactly when read); the stage ring keeps the type
+  const void* B;
+  void* C;        // FP64, or FP32 with out_f32
   int64_t K, lda, ldb, ldc;
   int M, N;
   double alpha, beta;
@@ -89,6 +89,7 @@ struct Args {
   double* partials;    // [nblk][nchunks][2][4096], then [nblk][15][4096] group sums
   unsigned* counter;   // tickets: [nblk][16] (15 groups + the block)
   int* err;
+  int out_f32;
 };
 
 // A' plane slot of digit plane p (p <= 0: zero planes), for the chain order above
@@ -118,6 +119,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 // arrive on the mbarrier once every cp.async of this thread so far has landed
 __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
@@ -182,7 +186,9 @@ __device__ __forceinline__ double pow2i(int e) {  // 2^e, clamped to the normal 
   return __hiloint2double((e + 1023) << 20, 0);
 }
 
+template <typename TI>
 __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
+  constexpr uint32_t ES = sizeof(TI);
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* raw_full = reinterpret_cast<uint64_t*>(smem);  // [MAXR]
   uint64_t* raw_empty = raw_full + MAXR;                   // [MAXR]
@@ -214,8 +220,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     bj = blk / p.bm;
   }
   const int Mb = min(W, p.M - W * bi), Nb = min(W, p.N - W * bj);
-  const double* Ab = p.A + W * bi;
-  const double* Bb = (p.sym ? p.A : p.B) + W * bj;
+  const TI* Ab = static_cast<const TI*>(p.A) + W * bi;
+  const TI* Bb = static_cast<const TI*>(p.sym ? p.A : p.B) + W * bj;
   const int64_t ldb = p.sym ? p.lda : p.ldb;
   const bool gram = p.sym && bi == bj;
   const int64_t s_begin = p.nstages * chunk / nchunks, s_end = p.nstages * (chunk + 1) / nchunks;
@@ -263,33 +269,39 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       }
       const int64_t row0 = (s_begin + ls) * ROWS;
       const int rows = (int)min((int64_t)ROWS, p.K - row0);
-      double* dA = reinterpret_cast<double*>(raw + (size_t)rs * p.raw_stage);
-      double* dB = dA + ROWS * W;
+      TI* dA = reinterpret_cast<TI*>(raw + (size_t)rs * p.raw_stage);
+      TI* dB = dA + ROWS * W;
       if (p.bulk) {
-        if (lane == 0) mbar_arrive_expect_tx(&raw_full[rs], (uint32_t)(rows * (Mb + (gram ? 0 : Nb)) * 8));
+        if (lane == 0) mbar_arrive_expect_tx(&raw_full[rs], (uint32_t)(rows * (Mb + (gram ? 0 : Nb)) * ES));
         __syncwarp();
         // dense rows (ld == block width): the stage is one contiguous copy; otherwise one per row
         if (dense_a) {
-          if (lane == 0) bulk_g2s(dA, Ab + row0 * p.lda, (uint32_t)(rows * Mb * 8), &raw_full[rs]);
+          if (lane == 0) bulk_g2s(dA, Ab + row0 * p.lda, (uint32_t)(rows * Mb * ES), &raw_full[rs]);
         } else if (lane < rows) {
-          bulk_g2s(dA + lane * W, Ab + (row0 + lane) * p.lda, (uint32_t)(Mb * 8), &raw_full[rs]);
+          bulk_g2s(dA + lane * W, Ab + (row0 + lane) * p.lda, (uint32_t)(Mb * ES), &raw_full[rs]);
         }
         if (!gram) {
           if (dense_b) {
-            if (lane == 1) bulk_g2s(dB, Bb + row0 * ldb, (uint32_t)(rows * Nb * 8), &raw_full[rs]);
+            if (lane == 1) bulk_g2s(dB, Bb + row0 * ldb, (uint32_t)(rows * Nb * ES), &raw_full[rs]);
           } else if (lane >= 16 && lane - 16 < rows) {
-            bulk_g2s(dB + (lane - 16) * W, Bb + (row0 + lane - 16) * ldb, (uint32_t)(Nb * 8), &raw_full[rs]);
+            bulk_g2s(dB + (lane - 16) * W, Bb + (row0 + lane - 16) * ldb, (uint32_t)(Nb * ES), &raw_full[rs]);
           }
         }
-      } else {  // rows not 16-byte aligned: 8-byte asynchronous copies, one arrival per lane
+      } else {  // rows not 16-byte aligned: element-sized asynchronous copies, one arrival per lane
         for (int e = lane; e < rows * Mb; e += 32) {
           const int r = e / Mb, c = e - r * Mb;
-          cp_async8(dA + r * W + c, Ab + (row0 + r) * p.lda + c);
+          if constexpr (ES == 8)
+            cp_async8(dA + r * W + c, Ab + (row0 + r) * p.lda + c);
+          else
+            cp_async4(dA + r * W + c, Ab + (row0 + r) * p.lda + c);
         }
         if (!gram)
           for (int e = lane; e < rows * Nb; e += 32) {
             const int r = e / Nb, c = e - r * Nb;
-            cp_async8(dB + r * W + c, Bb + (row0 + r) * ldb + c);
+            if constexpr (ES == 8)
+              cp_async8(dB + r * W + c, Bb + (row0 + r) * ldb + c);
+            else
+              cp_async4(dB + r * W + c, Bb + (row0 + r) * ldb + c);
           }
         cp_async_arrive(&raw_full[rs]);
       }
@@ -421,7 +433,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       }
       __syncwarp();
       // load my unit and its column maximum
-      const double* T = reinterpret_cast<const double*>(raw + (size_t)rs * p.raw_stage) + (isB ? ROWS * W : 0);
+      const TI* T = reinterpret_cast<const TI*>(raw + (size_t)rs * p.raw_stage) + (isB ? ROWS * W : 0);
       const int rstr = isB ? rsb : rsa;
       // column maximum of |x| from the high words (the exponent field of the largest high word is
       // the largest exponent field); nonzero low words mark subnormals in an otherwise zero column
@@ -430,7 +442,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         const int rr = sub * nrow + k;
-        v[k] = (k < nrow && cvalid && rr < rows) ? T[rr * rstr + c] : 0.0;
+        v[k] = (k < nrow && cvalid && rr < rows) ? (double)T[rr * rstr + c] : 0.0;
         mh = max(mh, (uint32_t)__double2hiint(v[k]) & 0x7FFFFFFFu);
         ol |= (uint32_t)__double2loint(v[k]);
       }
@@ -606,11 +618,16 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     double sum = 0.0;
 #pragma unroll
     for (int i = 0; i < 15; i++) sum += v[i];
-    double* cc = p.C + (int64_t)(W * bj + nn) * p.ldc + W * bi + mm;
-    *cc = p.beta_zero ? p.alpha * sum : (*cc) * p.beta + sum * p.alpha;
-    if (p.sym && bi < bj) {  // Gram: the mirrored block holds the same sums
-      double* cm = p.C + (int64_t)(W * bi + mm) * p.ldc + W * bj + nn;
-      *cm = p.beta_zero ? p.alpha * sum : (*cm) * p.beta + sum * p.alpha;
+    const int64_t ci = (int64_t)(W * bj + nn) * p.ldc + W * bi + mm, cmi = (int64_t)(W * bi + mm) * p.ldc + W * bj + nn;
+    const bool mirror = p.sym && bi < bj;  // Gram: the mirrored block holds the same sums
+    if (p.out_f32) {  // the one rounding of an FP32 result
+      float* C = static_cast<float*>(p.C);
+      C[ci] = (float)(p.beta_zero ? p.alpha * sum : (double)C[ci] * p.beta + sum * p.alpha);
+      if (mirror) C[cmi] = (float)(p.beta_zero ? p.alpha * sum : (double)C[cmi] * p.beta + sum * p.alpha);
+    } else {
+      double* C = static_cast<double*>(p.C);
+      C[ci] = p.beta_zero ? p.alpha * sum : C[ci] * p.beta + sum * p.alpha;
+      if (mirror) C[cmi] = p.beta_zero ? p.alpha * sum : C[cmi] * p.beta + sum * p.alpha;
     }
   }
   if (tid == 0) gcount[15] = 0u;
@@ -621,7 +638,14 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
 skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda,
                          const void* alpha, const double* B, int64_t ldb, const void* beta, double* C,
                          int64_t ldc, cudaStream_t st) {
+  return split_wide_t(h, false, false, M, N, K, A, lda, alpha, B, ldb, beta, C, ldc, st);
+}
+
+skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M, int64_t N, int64_t K,
+                           const void* A, int64_t lda, const void* alpha, const void* B, int64_t ldb,
+                           const void* beta, void* C, int64_t ldc, cudaStream_t st) {
   using namespace splitw;
+  const int64_t es = in_f32 ? 4 : 8;
   if (M > 128 || N > 128) {
     set_error("split precision TSMTTSM: M, N <= 128");
     return SKINNY_UNSUPPORTED;
@@ -636,15 +660,27 @@ skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const
   a.ldc = ldc;
   a.M = (int)M;
   a.N = (int)N;
-  std::memcpy(&a.alpha, alpha, 8);
-  std::memcpy(&a.beta, beta, 8);
+  if (out_f32) {  // FP32 scalars widened (exactly)
+    float af, bf;
+    std::memcpy(&af, alpha, 4);
+    std::memcpy(&bf, beta, 4);
+    a.alpha = af;
+    a.beta = bf;
+  } else {
+    std::memcpy(&a.alpha, alpha, 8);
+    std::memcpy(&a.beta, beta, 8);
+  }
+  a.out_f32 = out_f32;
   a.beta_zero = a.beta == 0.0;
   a.sym = (A == B) && (lda == ldb) && (M == N);
   a.bm = (int)((M + W - 1) / W);
   const int bn = (int)((N + W - 1) / W);
   a.nblk = a.sym ? a.bm * (a.bm + 1) / 2 : a.bm * bn;
-  const bool aligned = (uintptr_t)A % 16 == 0 && (uintptr_t)B % 16 == 0 && lda % 2 == 0 && ldb % 2 == 0;
-  a.bulk = aligned && M % 2 == 0 && N % 2 == 0;
+  // bulk copies: 16-byte aligned rows whose block widths are 16-byte multiples
+  const int64_t per16 = 16 / es;
+  const bool aligned =
+      (uintptr_t)A % 16 == 0 && (uintptr_t)B % 16 == 0 && lda % per16 == 0 && ldb % per16 == 0;
+  a.bulk = aligned && M % per16 == 0 && N % per16 == 0;
   a.raw_stage = (a.sym && a.nblk == 1) ? RAW_OP : 2 * RAW_OP;
   const int64_t fixed = HDR + (int64_t)DSLOTS * SLOT;
   a.rstages = (int)std::min<int64_t>(MAXR, (h->dev.smem_optin - fixed) / a.raw_stage);
@@ -663,9 +699,14 @@ skinny_status split_wide(skinny_handle h, int64_t M, int64_t N, int64_t K, const
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;
   a.err = h->err;
-  static SmemAttr attr;
-  ensure_smem_attr(split_wide_kernel, smem, attr);
-  split_wide_kernel<<<(int)grid, THREADS, smem, st>>>(a);
+  static SmemAttr attr, attr_f;
+  if (!in_f32) {
+    ensure_smem_attr(split_wide_kernel<double>, smem, attr);
+    split_wide_kernel<double><<<(int)grid, THREADS, smem, st>>>(a);
+  } else {
+    ensure_smem_attr(split_wide_kernel<float>, smem, attr_f);
+    split_wide_kernel<float><<<(int)grid, THREADS, smem, st>>>(a);
+  }
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

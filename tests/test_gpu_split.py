@@ -36,8 +36,8 @@ def test_split_golden_integer_cases_bit_exact(handle, case):
     assert np.array_equal(host(C), c["exp"])
 
 
-FP32_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and c["M"] <= (8 if c["cplx"] else 16) and
-              c["N"] <= (8 if c["cplx"] else 16)]
+FP32_CASES = [c for c in common.int_cases() if c["op"] == "tsmttsm" and c["M"] <= (64 if c["cplx"] else 128) and
+              c["N"] <= (64 if c["cplx"] else 128)]
 
 
 @pytest.mark.parametrize("case", FP32_CASES, ids=lambda c: c["id"])
@@ -54,14 +54,15 @@ def test_split_fp32_golden_integer_cases_bit_exact(handle, case):
 
 @pytest.mark.parametrize("dt", [np.float32, np.complex64])
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1000), (4, 4, 33333), (8, 8, 1 << 18), (16, 16, 50000), (3, 7, 4097),
-                                   (8, 2, 129)])
+                                   (8, 2, 129), (32, 32, 20000), (64, 64, 9000), (20, 41, 3001), (128, 16, 2000)])
 def test_split_fp32_vs_exact(handle, dt, M, N, K):
-    """FP32 / complex FP32 storage on the split kernel (exact products, FP64-accurate sums, one
+    """FP32 / complex FP32 storage on the split kernels (exact products, FP64-accurate sums, one
     rounding to FP32): within 2^-23 normwise of the exact result, where FP32 accumulation is held
-    to 8 sqrt(K) 2^-24.  Complex widths up to 8 (their real product is 16 wide)."""
+    to 8 sqrt(K) 2^-24.  Widths above 16 take the wide kernel (odd widths its element-wise copy
+    path); complex widths up to 64 (their real product is 128 wide)."""
     cplx = dt == np.complex64
-    if cplx and max(M, N) > 8:
-        pytest.skip("complex FP32 split TSMTTSM: M, N <= 8")
+    if cplx and max(M, N) > 64:
+        pytest.skip("complex split TSMTTSM: M, N <= 64")
     rng = np.random.default_rng(M * 31 + N * 7 + K + 5)
     lda, ldb, ldc = M, N, M + 2
     A = common.uniform(rng, K * lda, dt)
@@ -76,12 +77,20 @@ def test_split_fp32_vs_exact(handle, dt, M, N, K):
     assert err <= 2.0 ** -23, err
 
 
-def test_split_fp32_wide_is_refused(handle):
+def test_split_fp32_gram_and_beyond_the_limit(handle):
+    """FP32 Gram (A == B, mirrored 64 x 64 blocks) within the bound; widths above 128 refused."""
     from skinny_matmul_gb300 import SkinnyError
-    X = dev(np.zeros(64 * 64, np.float32))
-    C = dev(np.zeros(32 * 32, np.float32))
+    rng = np.random.default_rng(77)
+    M, K = 96, 5000
+    A = common.uniform(rng, K * M, np.float32)
+    Ad, Cd = dev(A), dev(np.zeros(M * M, np.float32))
+    handle.tsmttsm(M, M, K, Ad, M, 1.0, Ad, M, 0.0, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, M, K, A, M, A, M, np.zeros(M * M, np.float32), M, 1.0, 0.0)
+    assert common.normwise(host(Cd), exp, den) <= 2.0 ** -23
+    X = dev(np.zeros(130 * 64, np.float32))
+    C = dev(np.zeros(130 * 130, np.float32))
     with pytest.raises(SkinnyError, match="UNSUPPORTED"):
-        handle.tsmttsm(32, 32, 64, X, 32, 1.0, X[1:], 32, 0.0, C, 32, acc="split")
+        handle.tsmttsm(130, 130, 64, X, 130, 1.0, X[1:], 130, 0.0, C, 130, acc="split")
 
 
 SHAPES = [(1, 1, 1000), (2, 2, 70000), (4, 4, 33333), (8, 8, 1 << 20), (16, 16, 100000), (4, 16, 12345),
