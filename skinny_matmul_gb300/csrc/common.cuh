@@ -132,13 +132,19 @@ struct Ops<cplx<R>, cplx<R>> {
   }
   static __device__ __forceinline__ C add(C x, C y) { return {x.x + y.x, x.y + y.y}; }
   static __device__ __forceinline__ C mul(C a, C b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+  // r + beta * c: two FMAs for a real beta (the branch is uniform: beta is a launch argument),
+  // which matters where the FP64 pipe bounds the narrow complex TSMM
+  static __device__ __forceinline__ C add_beta_c(C r, C beta, C c) {
+    if (beta.y == R(0)) return {fma(beta.x, c.x, r.x), fma(beta.x, c.y, r.y)};
+    return add(mul(beta, c), r);
+  }
   static __device__ __forceinline__ C finish(C s, C alpha, C beta, bool beta_zero, const C* c) {
     C r = mul(alpha, s);
-    if (!beta_zero) r = add(mul(beta, *c), r);
+    if (!beta_zero) r = add_beta_c(r, beta, *c);
     return r;
   }
   static __device__ __forceinline__ C finish1(C s, C beta, bool beta_zero, const C* c) {
-    return beta_zero ? s : add(mul(beta, *c), s);
+    return beta_zero ? s : add_beta_c(s, beta, *c);
   }
   static __device__ __forceinline__ bool is_one(C a) { return a.x == R(1) && a.y == R(0); }
   static __device__ __forceinline__ C shfl_xor(C v, int o) {
