@@ -1,7 +1,7 @@
 // svqb_host_dd.cu -- SVQB in double-double on the host (the reference's high-precision study,
 // svqb/svqb.cu:132-182 svqb_xd<dd_real>, which calls MPACK's Rgemm / Rsyev).  Host code only:
-// the accuracy baseline against which the device SVQB (svqb.cu) is judged at high condition
-// numbers, where a one-pass FP64 SVQB loses orthogonality as kappa^2 u.
+// the accuracy baseline for the device SVQB (svqb.cu) at high condition numbers, where a
+// one-pass FP64 SVQB loses orthogonality as kappa^2 u.
 //
 // Steps as in the reference, every one in double-double:
 //   S = X^T X; d_i = 1/sqrt(S_ii) (0 when S_ii <= eps, eps the double-double epsilon 2^-104);

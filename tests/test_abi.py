@@ -79,7 +79,7 @@ def test_launcher_list_shape():
 
 def test_cpp_shim_header_compiles():
     """include/skinny.hpp (the reference's launcher spellings) compiles as C++17 against the CUDA
-    headers, together with the driver the GPU test runs."""
+    headers, together with the C++ test program the GPU test runs."""
     import shutil
     import subprocess
     gxx = shutil.which("g++")
