@@ -172,10 +172,29 @@ def tsmttsm_sweep_items():
     return items
 
 
+def launch_time(fn, reps):
+    """Mean device seconds of fn(1)..fn(reps), launched back to back on the current stream.  fn(0)
+    runs first, untimed, and keeps the GPU busy while the timed launches are enqueued, so the
+    events bracket device work only: a launch timed alone on an idle GPU would also count the
+    host's call path (~20 us through Python), which is a fifth of a 100 us product.  Returns None
+    when a call returns False (a launcher that refused the shape)."""
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ok = fn(0) is not False
+    e0.record()
+    for i in range(1, reps + 1):
+        ok = (fn(i) is not False) and ok
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3 / reps if ok else None
+
+
 def tsmttsm_sweep(h, dev, reps=5):
     """The metric's TSMTTSM half: every shape of tsmttsm_sweep_items() plus C1 (8 x 8, K = 2^20, 16
     rotating input copies so the inputs exceed L2), each with the library's choice (auto) and the
-    CUDA-core FP64 kernel (native); median of `reps` CUDA-event timings after two warm-ups."""
+    CUDA-core FP64 kernel (native): after two warm-ups, the mean device time of `reps` launches
+    timed back to back with CUDA events (launch_time)."""
     import torch
     hbm, _ = peaks()
     rows = []
@@ -185,15 +204,7 @@ def tsmttsm_sweep(h, dev, reps=5):
         for method in ("auto", "native"):
             for i in range(2):
                 call(h, it, ops, i, method)
-            ts = []
-            for i in range(reps):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                call(h, it, ops, i, method)
-                e1.record()
-                e1.synchronize()
-                ts.append(e0.elapsed_time(e1) * 1e-3)
-            t = sorted(ts)[len(ts) // 2]
+            t = launch_time(lambda i: call(h, it, ops, i, method), reps)
             gbs = it["bytes"] / t / 1e9
             row[method] = {"us": round(t * 1e6, 1), "GB/s": round(gbs, 1), "hbm_frac": round(gbs / hbm, 4),
                            "fp64_equivalent_tflops": round(it["flops"] / t / 1e12, 3),
@@ -310,7 +321,7 @@ def kernel_of(it, method):
         wide = Mr > 16 or Nr > 16
         nblk = ((Mr + 63) // 64) * ((Nr + 63) // 64)
         auto_split = K >= 4096 and (Mr * Nr >= 256 or (Mr >= 8 and Nr >= 8)) and \
-            (not wide or Mr * Nr >= 320 * nblk)
+            (not wide or Mr * Nr >= (160 if Mr <= 32 and Nr <= 32 else 320) * nblk)
         if fp64 and (method == "split" or (method == "auto" and auto_split)):
             return "split_wide_kernel" if wide else "split_tsmttsm_kernel"
         p2 = lambda x: 1 << (x - 1).bit_length()
@@ -473,24 +484,17 @@ def reference_gpu_kernels(items, reps=3):
         best = {}
         for v in variants:
             for bc in ([sms] if v == "FIX_IP_GHOST" else [sms * m for m in range(1, 9)]):
-                ts = []
-                for r in range(reps + 1):
-                    j = r % copies
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record()
+                def one(r):
                     if tsmm:
-                        ok = ref_gpu.tsmm(v, M, N, K, A[0], M, 1.0, B[0], M, 0.5, C, M if it["inplace"] else N, bc)
-                    else:
-                        ok = ref_gpu.tsmttsm(v, M, N, K, A[j], M, 1.0, B[j], N, 0.0, C, M, bc, temp=temp)
-                    e1.record()
-                    e1.synchronize()
-                    if not ok:
-                        break
-                    if r:
-                        ts.append(e0.elapsed_time(e1) * 1e-3)
-                if not ts:
+                        return ref_gpu.tsmm(v, M, N, K, A[0], M, 1.0, B[0], M, 0.5, C, M if it["inplace"] else N,
+                                            bc)
+                    return ref_gpu.tsmttsm(v, M, N, K, A[r % copies], M, 1.0, B[r % copies], N, 0.0, C, M, bc,
+                                           temp=temp)
+                if not one(0):
                     continue
-                t = sorted(ts)[len(ts) // 2]
+                t = launch_time(one, reps)
+                if t is None:
+                    continue
                 if v not in best or t < best[v][0]:
                     best[v] = (t, bc)
         del A, B, C, temp

@@ -44,6 +44,11 @@
 //   * Blocks of 64 x 64 (M or N > 64) run in the same launch, as do the row chunks of every
 //     block; the last CTA of a block (ticket) sums the chunks' partials in chunk order and
 //     applies alpha and beta.  Gram (A = B) computes the upper blocks only and mirrors them.
+//   * Folded stages (M, N <= 32): a stage holds 32 rows; rows 0..15 fill plane rows 0..31 and
+//     rows 16..31 fill plane rows 32..63 (column c of row 16 + r is plane row 32 + c).  The
+//     diagonal quadrants of the 64 x 64 accumulators then hold the sums over the two row halves
+//     (the off-diagonal quadrants pair different rows and are not read), so a 32-wide product
+//     uses every slicer and every MMA column, and the halves are added at the end.
 // Inputs must be finite (Inf/NaN have no fixed-point form).
 #include <cuda_fp16.h>
 
@@ -85,7 +90,7 @@ struct Args {
   int bulk;           // rows by bulk copy (16-byte aligned rows of even width)
   int rstages;
   uint32_t raw_stage;  // bytes per FP64 stage
-  int64_t nstages;     // ceil(K / ROWS)
+  int64_t nstages;     // ceil(K / rows per stage)
   double* partials;    // [nblk][nchunks][2][4096], then [nblk][15][4096] group sums
   unsigned* counter;   // tickets: [nblk][16] (15 groups + the block)
   int* err;
@@ -186,7 +191,7 @@ __device__ __forceinline__ double pow2i(int e) {  // 2^e, clamped to the normal 
   return __hiloint2double((e + 1023) << 20, 0);
 }
 
-template <typename TI>
+template <typename TI, bool FOLD>
 __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
   constexpr uint32_t ES = sizeof(TI);
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -229,7 +234,10 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
   const int R = p.rstages;
   // row strides (doubles) of the FP64 stages: dense operands land as one block of rows
   const bool dense_a = p.bulk && p.lda == Mb, dense_b = p.bulk && ldb == Nb;
-  const int rsa = dense_a ? Mb : W, rsb = dense_b ? Nb : W;
+  // rows per stage; row stride of the stage's rows that are copied one by one (a folded stage
+  // holds 32 rows of at most 32 values in the same 16 x 64 space)
+  const int SR = FOLD ? 2 * ROWS : ROWS, rw = FOLD ? W / 2 : W;
+  const int rsa = dense_a ? Mb : rw, rsb = dense_b ? Nb : rw;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot)));
@@ -267,41 +275,38 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
         if (lane == 0) ok = wait_ab(&raw_empty[rs], (uint32_t)((use - 1) & 1), abort_f, p.err, 64);
         if (!__shfl_sync(0xffffffffu, ok, 0)) break;
       }
-      const int64_t row0 = (s_begin + ls) * ROWS;
-      const int rows = (int)min((int64_t)ROWS, p.K - row0);
+      const int64_t row0 = (s_begin + ls) * SR;
+      const int rows = (int)min((int64_t)SR, p.K - row0);
       TI* dA = reinterpret_cast<TI*>(raw + (size_t)rs * p.raw_stage);
       TI* dB = dA + ROWS * W;
       if (p.bulk) {
         if (lane == 0) mbar_arrive_expect_tx(&raw_full[rs], (uint32_t)(rows * (Mb + (gram ? 0 : Nb)) * ES));
         __syncwarp();
         // dense rows (ld == block width): the stage is one contiguous copy; otherwise one per row
-        if (dense_a) {
-          if (lane == 0) bulk_g2s(dA, Ab + row0 * p.lda, (uint32_t)(rows * Mb * ES), &raw_full[rs]);
-        } else if (lane < rows) {
-          bulk_g2s(dA + lane * W, Ab + (row0 + lane) * p.lda, (uint32_t)(Mb * ES), &raw_full[rs]);
-        }
-        if (!gram) {
-          if (dense_b) {
-            if (lane == 1) bulk_g2s(dB, Bb + row0 * ldb, (uint32_t)(rows * Nb * ES), &raw_full[rs]);
-          } else if (lane >= 16 && lane - 16 < rows) {
-            bulk_g2s(dB + (lane - 16) * W, Bb + (row0 + lane - 16) * ldb, (uint32_t)(Nb * ES), &raw_full[rs]);
-          }
+        if (dense_a && lane == 0) bulk_g2s(dA, Ab + row0 * p.lda, (uint32_t)(rows * Mb * ES), &raw_full[rs]);
+        if (!gram && dense_b && lane == 1) bulk_g2s(dB, Bb + row0 * ldb, (uint32_t)(rows * Nb * ES), &raw_full[rs]);
+        const int na = dense_a ? 0 : rows, nb = (gram || dense_b) ? 0 : rows;
+        for (int r = lane; r < na + nb; r += 32) {
+          if (r < na)
+            bulk_g2s(dA + r * rw, Ab + (row0 + r) * p.lda, (uint32_t)(Mb * ES), &raw_full[rs]);
+          else
+            bulk_g2s(dB + (r - na) * rw, Bb + (row0 + r - na) * ldb, (uint32_t)(Nb * ES), &raw_full[rs]);
         }
       } else {  // rows not 16-byte aligned: element-sized asynchronous copies, one arrival per lane
         for (int e = lane; e < rows * Mb; e += 32) {
           const int r = e / Mb, c = e - r * Mb;
           if constexpr (ES == 8)
-            cp_async8(dA + r * W + c, Ab + (row0 + r) * p.lda + c);
+            cp_async8(dA + r * rw + c, Ab + (row0 + r) * p.lda + c);
           else
-            cp_async4(dA + r * W + c, Ab + (row0 + r) * p.lda + c);
+            cp_async4(dA + r * rw + c, Ab + (row0 + r) * p.lda + c);
         }
         if (!gram)
           for (int e = lane; e < rows * Nb; e += 32) {
             const int r = e / Nb, c = e - r * Nb;
             if constexpr (ES == 8)
-              cp_async8(dB + r * W + c, Bb + (row0 + r) * ldb + c);
+              cp_async8(dB + r * rw + c, Bb + (row0 + r) * ldb + c);
             else
-              cp_async4(dB + r * W + c, Bb + (row0 + r) * ldb + c);
+              cp_async4(dB + r * rw + c, Bb + (row0 + r) * ldb + c);
           }
         cp_async_arrive(&raw_full[rs]);
       }
@@ -351,13 +356,18 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     const int c = gram ? 8 * warp + (lane & 7) : 16 * (warp & 3) + (lane & 15);
     const int sub = gram ? (lane >> 3) : (lane >> 4);
     const int nrow = gram ? 4 : 8;
-    const bool cvalid = c < (isB ? Nb : Mb);
+    // folded stages: plane row c holds column c % 32 of the stage's row half c / 32
+    const int cact = FOLD ? (c & 31) : c, rbase = FOLD ? ROWS * (c >> 5) : 0;
+    const bool cvalid = cact < (isB ? Nb : Mb);
     const int cofs = (c >> 3) * 128 + (c & 7) * 16;  // row c of a digit plane (8-row core groups)
     uint32_t Ecur = 0;
     // drain cells: TMEM lane 32 q + lane (q = warp % 4), C column block [32 nh, 32 nh + 32)
     const int q = warp & 3, nh = warp >> 2;
     const int hm = q >> 1;                  // 0: levels 2..5, 1: levels 6..9
     const int m = (32 * q + lane) & 63;
+    // cells this thread keeps: folded stages keep the two diagonal quadrants only
+    const bool live = !FOLD || (q & 1) == nh;
+    const int mv = FOLD ? (m & 31) : m, nofs = FOLD ? 32 * nh : 0;
     long long acc[32];
 #pragma unroll
     for (int x = 0; x < 32; x++) acc[x] = 0;
@@ -370,7 +380,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
 #pragma unroll
       for (int x = 0; x < 32; x++) {
         const int n = 32 * nh + x;
-        if (m < Mb && n < Nb) {
+        if (live && mv < Mb && n - nofs < Nb) {
           double v = 0.0;
           if (acc_epoch >= 0)
             v = (double)acc[x] * pow2i(ea - 1040) * pow2i(acc_rec[64 + n] - 1040 - (hm ? 32 : 0));
@@ -398,7 +408,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + buf * 256 + 32 * nh;
 #pragma unroll
       for (int hp = 0; hp < 4; hp++) {
-        if (hp != k) continue;
+        if (hp != k || !live) continue;
         uint32_t s0[8], s1[8], s2[8], s3[8];
         tmem_ld8(tb + hp * 8, s0);          // key 2, columns j   : level 2 / 6
         tmem_ld8(tb + 64 + hp * 8, s1);     // key 2, columns j+1 : level 3 / 7
@@ -423,8 +433,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
     int pend = 0, pend_buf = 0, pend_last = 0, pend_piece = 0;
     for (int ls = 0; ls < nst; ls++) {
       const int rs = ls % R, ds = ls % DSLOTS;
-      const int64_t row0 = (s_begin + ls) * ROWS;
-      const int rows = (int)min((int64_t)ROWS, p.K - row0);
+      const int64_t row0 = (s_begin + ls) * SR;
+      const int rows = (int)min((int64_t)SR, p.K - row0);
       // lane 0 waits for the FP64 stage (TMA) and for the MMAs that read the digit slot; the
       // warp barrier then orders the other lanes' reads and writes after those waits
       if (lane == 0) {
@@ -441,8 +451,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       uint32_t mh = 0, ol = 0;
 #pragma unroll
       for (int k = 0; k < 8; k++) {
-        const int rr = sub * nrow + k;
-        v[k] = (k < nrow && cvalid && rr < rows) ? (double)T[rr * rstr + c] : 0.0;
+        const int rr = rbase + sub * nrow + k;
+        v[k] = (k < nrow && cvalid && rr < rows) ? (double)T[rr * rstr + cact] : 0.0;
         mh = max(mh, (uint32_t)__double2hiint(v[k]) & 0x7FFFFFFFu);
         ol |= (uint32_t)__double2loint(v[k]);
       }
@@ -562,13 +572,19 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
       for (int k = 0; k < 4; k++) drain_piece(cur_buf, k);
     }
     flush();
-    // the CTA's sum of a cell: levels 2..5 (half 0) plus levels 6..9 (half 1), into half 0
+    // the CTA's sum of a cell: levels 2..5 (half 0) plus levels 6..9 (half 1), into half 0; with
+    // folded stages the second row half's quadrant is then added to the first's
     slicers_sync();
-    if (hm == 0 && m < Mb)
+    if (hm == 0 && live && mv < Mb)
       for (int x = 0; x < 32; x++) {
         const int n = 32 * nh + x;
-        if (n < Nb) part[n * 64 + m] += part[4096 + n * 64 + m];
+        if (n - nofs < Nb) part[n * 64 + m] += part[4096 + n * 64 + m];
       }
+    if constexpr (FOLD) {
+      slicers_sync();
+      if (hm == 0 && nh == 0 && q == 0 && m < Mb)
+        for (int x = 0; x < Nb; x++) part[x * 64 + m] += part[(x + 32) * 64 + m + 32];
+    }
   }
 
   tc_before();
@@ -682,6 +698,7 @@ skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M
       (uintptr_t)A % 16 == 0 && (uintptr_t)B % 16 == 0 && lda % per16 == 0 && ldb % per16 == 0;
   a.bulk = aligned && M % per16 == 0 && N % per16 == 0;
   a.raw_stage = (a.sym && a.nblk == 1) ? RAW_OP : 2 * RAW_OP;
+  const bool fold = M <= W / 2 && N <= W / 2;  // 32-row stages folded into the 64-row planes
   const int64_t fixed = HDR + (int64_t)DSLOTS * SLOT;
   a.rstages = (int)std::min<int64_t>(MAXR, (h->dev.smem_optin - fixed) / a.raw_stage);
   if (a.rstages < 2) {
@@ -689,7 +706,8 @@ skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M
     return SKINNY_UNSUPPORTED;
   }
   const int smem = (int)(fixed + (int64_t)a.rstages * a.raw_stage);
-  a.nstages = (K + ROWS - 1) / ROWS;
+  const int64_t srows = fold ? 2 * ROWS : ROWS;
+  a.nstages = (K + srows - 1) / srows;
   const int64_t nchunks = std::max<int64_t>(1, std::min<int64_t>({a.nstages, h->dev.sms / a.nblk,
                                                                    (int64_t)15 * GROUP}));
   const int64_t grid = nchunks * a.nblk;
@@ -699,14 +717,15 @@ skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;
   a.err = h->err;
-  static SmemAttr attr, attr_f;
-  if (!in_f32) {
-    ensure_smem_attr(split_wide_kernel<double>, smem, attr);
-    split_wide_kernel<double><<<(int)grid, THREADS, smem, st>>>(a);
-  } else {
-    ensure_smem_attr(split_wide_kernel<float>, smem, attr_f);
-    split_wide_kernel<float><<<(int)grid, THREADS, smem, st>>>(a);
-  }
+  static SmemAttr attr[4];
+  auto launch = [&](auto kernel, SmemAttr& at) {
+    ensure_smem_attr(kernel, smem, at);
+    kernel<<<(int)grid, THREADS, smem, st>>>(a);
+  };
+  if (!in_f32)
+    fold ? launch(split_wide_kernel<double, true>, attr[0]) : launch(split_wide_kernel<double, false>, attr[1]);
+  else
+    fold ? launch(split_wide_kernel<float, true>, attr[2]) : launch(split_wide_kernel<float, false>, attr[3]);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -54,7 +54,8 @@ def test_split_fp32_golden_integer_cases_bit_exact(handle, case):
 
 @pytest.mark.parametrize("dt", [np.float32, np.complex64])
 @pytest.mark.parametrize("M,N,K", [(1, 1, 1000), (4, 4, 33333), (8, 8, 1 << 18), (16, 16, 50000), (3, 7, 4097),
-                                   (8, 2, 129), (32, 32, 20000), (64, 64, 9000), (20, 41, 3001), (128, 16, 2000)])
+                                   (8, 2, 129), (32, 32, 20000), (64, 64, 9000), (20, 41, 3001), (128, 16, 2000),
+                                   (24, 19, 5001)])
 def test_split_fp32_vs_exact(handle, dt, M, N, K):
     """FP32 / complex FP32 storage on the split kernels (exact products, FP64-accurate sums, one
     rounding to FP32): within 2^-23 normwise of the exact result, where FP32 accumulation is held
@@ -200,6 +201,72 @@ def test_split_blocked_vs_exact(handle, M, N, K, pad):
     err = common.normwise(got, exp, den, common.c_mask_tsmttsm(M, N, ldc))
     assert err <= 4e-16, err
     assert np.array_equal(got[~common.c_mask_tsmttsm(M, N, ldc)], C0[~common.c_mask_tsmttsm(M, N, ldc)])
+
+
+# M, N <= 32 with one of them > 16: the wide kernel's folded stages (32 rows per stage; rows
+# 16..31 fill the second half of the 64-row digit planes, the two diagonal quadrants are added)
+FOLDED = [(17, 17, 1001), (32, 8, 40001), (24, 31, 4097), (20, 1, 3000), (32, 32, 65), (29, 18, 33),
+          (1, 32, 777)]
+
+
+@pytest.mark.parametrize("M,N,K", FOLDED)
+@pytest.mark.parametrize("pad", [0, 1, 2])
+def test_split_folded_vs_exact(handle, M, N, K, pad):
+    """The same bars as the blocked shapes, for every copy path (dense, 8-byte, per-row bulk)."""
+    rng = np.random.default_rng(M * 17 + N * 5 + K + pad)
+    lda, ldb, ldc = M + pad, N + pad, M + 1
+    A = rng.uniform(-1, 1, K * lda)
+    B = rng.uniform(-1, 1, K * ldb)
+    C0 = rng.uniform(-1, 1, N * ldc)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), lda, -1.25, dev(B), ldb, 0.5, Cd, ldc, acc="split")
+    got = host(Cd)
+    exp, den = common.tsmttsm_expected(M, N, K, A, lda, B, ldb, C0, ldc, -1.25, 0.5)
+    mask = common.c_mask_tsmttsm(M, N, ldc)
+    assert common.normwise(got, exp, den, mask) <= 4e-16
+    assert np.array_equal(got[~mask], C0[~mask])
+
+
+@pytest.mark.parametrize("K", [1, 15, 16, 17, 31, 32, 33, 255, 256, 257, 4095, 4097])
+def test_split_folded_small_k(handle, K):
+    rng = np.random.default_rng(K + 3)
+    M, N = 32, 20
+    A, B = rng.uniform(-1, 1, K * M), rng.uniform(-1, 1, K * N)
+    C0 = rng.uniform(-1, 1, M * N)
+    Cd = dev(C0)
+    handle.tsmttsm(M, N, K, dev(A), M, 2.0, dev(B), N, 0.5, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, N, K, A, M, B, N, C0, M, 2.0, 0.5)
+    assert common.normwise(host(Cd), exp, den) <= 4e-16
+
+
+def test_split_folded_row_halves_with_different_exponents(handle):
+    """Rows 16..31 of every 32-row stage are 2^12 larger than rows 0..15, and the scale grows
+    along K: the two plane halves of a column carry different exponents and start new epochs at
+    different stages.  Gram of the same data is mirrored and deterministic."""
+    rng = np.random.default_rng(5)
+    M, N, K = 24, 32, 90001
+    k = np.arange(K)
+    scale = np.ldexp(1.0, 12 * ((k // 16) % 2) + (k // 9000) - 5)
+    A = (rng.uniform(-1, 1, (K, M)) * scale[:, None])
+    B = rng.uniform(-1, 1, (K, N))
+    A[:, 3] = 0.0
+    B[: K // 3, 30] = 0.0
+    A, B = A.ravel(), B.ravel()
+    Cd = dev(np.zeros(M * N))
+    handle.tsmttsm(M, N, K, dev(A), M, 1.0, dev(B), N, 0.0, Cd, M, acc="split")
+    exp, den = common.tsmttsm_expected(M, N, K, A, M, B, N, np.zeros(M * N), M, 1.0, 0.0)
+    assert common.normwise(host(Cd), exp, den) <= 4e-16
+    Ad = dev(A)
+    outs = []
+    for _ in range(2):
+        Gd = dev(np.zeros(M * M))
+        handle.tsmttsm(M, M, K, Ad, M, 1.0, Ad, M, 0.0, Gd, M, acc="split")
+        outs.append(host(Gd))
+    assert np.array_equal(outs[0], outs[1])
+    G = outs[0].reshape(M, M)
+    assert np.array_equal(G, G.T)
+    exp, den = common.tsmttsm_expected(M, M, K, A, M, A, M, np.zeros(M * M), M, 1.0, 0.0)
+    assert common.normwise(outs[0], exp, den) <= 4e-16
 
 
 @pytest.mark.parametrize("M", [17, 32, 40, 64, 128])
