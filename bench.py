@@ -256,6 +256,13 @@ def probe_split_wide_items():
                  flops=2 * M * N * K, copies=1)]
 
 
+def probe_split_wide32_items():
+    M = N = 32
+    K = 1 << 22
+    return [dict(op="tsmttsm", dt="f64", M=M, N=N, K=K, inplace=False, s=8, bytes=(M + N) * K * 8,
+                 flops=2 * M * N * K, copies=1)]
+
+
 WORKLOADS = {
     "probe-split-tsmm64": (probe_tsmm64_items, "TSMM FP64 64x64, K = 2^20 (512 MiB A), alpha 1, beta 0.5, run "
                            "with --method split: small case for ncu"),
@@ -263,6 +270,8 @@ WORKLOADS = {
     "probe-split": (probe_split_items, "TSMTTSM FP64 8x8, K = 2^22, run with --method split: small case for ncu"),
     "probe-split-wide": (probe_split_wide_items, "TSMTTSM FP64 64x64, K = 2^21 (2 x 1 GiB), run with --method "
                          "split: small case for ncu"),
+    "probe-split-wide32": (probe_split_wide32_items, "TSMTTSM FP64 32x32, K = 2^22 (2 x 1 GiB), run with --method "
+                           "split: folded stages, small case for ncu"),
     "probe-tsmm": (probe_tsmm_items, "TSMM FP64 8x8, K = 2^22 (256 MiB A), alpha 1, beta 0.5: small case for ncu"),
     "probe-tsmttsm": (probe_tsmttsm_items, "TSMTTSM FP64 8x8, K = 2^22 (2 x 256 MiB): small case for ncu"),
     "probe-tsmttsm1": (probe_tsmttsm1_items, "TSMTTSM FP64 1x1, K = 2^25 (2 x 256 MiB): small case for ncu"),

@@ -66,6 +66,8 @@ constexpr int STATIC_RESERVE = 1024;     // the kernel's static shared memory
 constexpr uint32_t SLEEP_DRAIN = 256;    // ns between polls of the drain warps (a period is ~8 rounds)
 constexpr uint32_t SLEEP_PRODUCER = 64;  // ns between polls of the producer warp
 constexpr uint32_t SLEEP_MMA = 32;       // ns between polls of the MMA thread
+constexpr int GROUP = 16;                // CTAs per first-level group of the cross-CTA finish
+constexpr int MAXGROUPS = 16;            // groups at most (grid <= 256); counter[MAXGROUPS] is the last level's
 
 struct Args {
   const void* A;  // FP64, or FP32 with in_f32 (widened exactly when read)
@@ -194,6 +196,19 @@ __device__ __forceinline__ int drainers_any(int pred) {
   return r;
 }
 __device__ __forceinline__ void drainers_sync() { asm volatile("bar.sync 2, 128;" ::: "memory"); }
+
+// Sum of c[t] over the lanes that hold the same column m of A (lane = (i0, m), MP lanes per
+// digit): xor-shuffles at distances MP..16, the eight levels' shuffles of a stage issued together
+// so that their latencies overlap.
+__device__ __forceinline__ void level_reduce(int (&c)[DIGITS], int MP) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    if (o >= MP) {  // warp-uniform
+#pragma unroll
+      for (int t = 0; t < DIGITS; t++) c[t] += __shfl_xor_sync(0xffffffffu, c[t], o);
+    }
+  }
+}
 
 // bounded wait that also gives up as soon as another thread of the CTA has given up; sleep_ns
 // between polls for the roles that wait most of the time
@@ -411,11 +426,13 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
               for (int t = 0; t < DIGITS; t++) R[t] = T[t];
             }
           }
+          int c[DIGITS];
 #pragma unroll
-          for (int t = 0; t < DIGITS; t++) {
-            int c = (i0 <= t) ? R[t] : 0;
-            for (int o = MP; o < 32; o <<= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-            if (lane < MP && rvalid && n < N) atomicAdd(&S[(t * 16 + m) * 16 + n], c);
+          for (int t = 0; t < DIGITS; t++) c[t] = (i0 <= t) ? R[t] : 0;
+          level_reduce(c, MP);
+          if (lane < MP && rvalid && n < N) {
+#pragma unroll
+            for (int t = 0; t < DIGITS; t++) atomicAdd(&S[(t * 16 + m) * 16 + n], c[t]);
           }
         }
       }
@@ -559,30 +576,46 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols));
   if (*abort_f) return;  // timeout recorded in the error word; no partial, no ticket
 
-  // ---- cross-CTA finish -----------------------------------------------------------------------
+  // ---- cross-CTA finish, two levels: the last CTA of each group of GROUP CTAs sums the group's
+  // partials in CTA order, the last group to finish sums the group sums in group order and applies
+  // alpha and beta (deterministic; each level is one round of independent loads) -----------------
   const int MN = M * N;
   if (tid < MN) p.partials[(size_t)chunk * MN + tid] = cacc[tid];
   __threadfence();
   __syncthreads();
   __shared__ int s_last;
-  if (tid == 0) s_last = (atomicAdd(p.counter, 1u) == (unsigned)(nchunks - 1));
+  const int ngroups = (nchunks + GROUP - 1) / GROUP, grp = chunk / GROUP;
+  const int gsize = min(GROUP, nchunks - grp * GROUP);
+  if (tid == 0) s_last = (atomicAdd(p.counter + grp, 1u) == (unsigned)(gsize - 1));
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  double* red = reinterpret_cast<double*>(ring);
-  const int P = THREADS / MN;  // >= 1 since MN <= 256
-  const int e = tid % MN, j = tid / MN;
-  if (j < P) {
+  double* Gs = p.partials + (size_t)nchunks * MN;  // [group][MN]
+  for (int e = tid; e < MN; e += THREADS) {
+    double v[GROUP];
+#pragma unroll
+    for (int i = 0; i < GROUP; i++) v[i] = i < gsize ? __ldcg(&p.partials[(size_t)(grp * GROUP + i) * MN + e]) : 0.0;
     double sum = 0.0;
-    const int b0 = (int)((int64_t)nchunks * j / P), b1 = (int)((int64_t)nchunks * (j + 1) / P);
-#pragma unroll 8
-    for (int bb = b0; bb < b1; bb++) sum += __ldcg(&p.partials[(size_t)bb * MN + e]);  // loads overlap
-    red[j * MN + e] = sum;
+#pragma unroll
+    for (int i = 0; i < GROUP; i++) sum += v[i];
+    Gs[(size_t)grp * MN + e] = sum;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    p.counter[grp] = 0u;
+    s_last = (atomicAdd(p.counter + MAXGROUPS, 1u) == (unsigned)(ngroups - 1));
   }
   __syncthreads();
+  if (!s_last) return;
+  __threadfence();
   if (tid < MN) {
-    double sum = red[tid];
-    for (int q2 = 1; q2 < P; q2++) sum += red[q2 * MN + tid];
+    double v[MAXGROUPS];
+#pragma unroll
+    for (int i = 0; i < MAXGROUPS; i++) v[i] = i < ngroups ? __ldcg(&Gs[(size_t)i * MN + tid]) : 0.0;
+    double sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < MAXGROUPS; i++) sum += v[i];
     const int mm = tid % M, nn = tid / M;
     const int64_t ci = (int64_t)nn * p.ldc + mm;
     if (p.out_f32) {  // the one rounding of an FP32 result
@@ -593,7 +626,7 @@ __global__ void __launch_bounds__(THREADS, 1) split_tsmttsm_kernel(const Args p)
       *c = p.beta_zero ? p.alpha * sum : (*c) * p.beta + sum * p.alpha;
     }
   }
-  if (tid == 0) *p.counter = 0u;
+  if (tid == 0) p.counter[MAXGROUPS] = 0u;
 }
 
 template <int NP, typename TI>
@@ -720,9 +753,10 @@ skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_
   a.nrounds = (K + a.rr - 1) / a.rr;
   const int smem2 =
       (int)(fixed - STATIC_RESERVE + (int64_t)a.stages * a.stage_bytes + (int64_t)a.dstages * dstage);
-  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(a.nrounds, h->dev.sms));
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>({a.nrounds, h->dev.sms, (int64_t)GROUP * MAXGROUPS}));
   Workspace& ws = h->ws[st];
-  skinny_status s = workspace_ensure(ws, (size_t)grid * M * N * 8, st);
+  // CTA partials, then the group sums
+  skinny_status s = workspace_ensure(ws, ((size_t)grid + MAXGROUPS) * M * N * 8, st);
   if (s != SKINNY_OK) return s;
   a.partials = (double*)ws.partials;
   a.counter = ws.counter;
