@@ -240,16 +240,27 @@ __device__ __forceinline__ int f32_int23_near(float f) { return 2 * (__float_as_
 // The double W * 2^(er + fc - 2100) then comes from one of two finishers (same accuracy): the
 // integer one runs on the ALU pipe, the conversion one on the FP64 pipe, which is free for it
 // when the epilogue has no beta FMA.  W == 0 and results below the normal range give 0.
+// A pair of levels within 2^22 takes one multiply-add on the magic-number bit patterns: with
+// b = 0x4B400000 + D, b0 * 256 + b1 = D0 * 256 + D1 + 0x8B400000 modulo 2^32 (0x4B400000 * 256 is
+// 0x40000000 modulo 2^32), and |D0 * 256 + D1| < 2^31 makes the signed difference exact.
+__device__ __forceinline__ int pair22(float f0, float f1) {
+  const uint32_t b0 = __float_as_uint(f0 + 12582912.0f), b1 = __float_as_uint(f1 + 12582912.0f);
+  return (int)(b0 * 256u + b1 - 0x8B400000u);
+}
 template <int MP, int W>
 __device__ __forceinline__ long long level_window(const uint32_t (&raw)[8][W], int x) {
-  int d[8];
+  float f[8];
 #pragma unroll
-  for (int L = 0; L < 8; L++) {
-    const float f = __uint_as_float(raw[L][x]);
-    d[L] = (MP <= 32 || L < 5) ? f32_int22(f) : (L == 5 ? f32_int24(f) : f32_int23_near(f));
+  for (int L = 0; L < 8; L++) f[L] = __uint_as_float(raw[L][x]);
+  const int P1 = pair22(f[0], f[1]), P2 = pair22(f[2], f[3]);
+  int P3, P4;
+  if constexpr (MP <= 32) {
+    P3 = pair22(f[4], f[5]);
+    P4 = pair22(f[6], f[7]);
+  } else {
+    P3 = f32_int22(f[4]) * 256 + f32_int24(f[5]);
+    P4 = f32_int23_near(f[6]) * 256 + f32_int23_near(f[7]);
   }
-  const int P1 = d[0] * 256 + d[1], P2 = d[2] * 256 + d[3];
-  const int P3 = d[4] * 256 + d[5], P4 = d[6] * 256 + d[7];
   return ((long long)P1 << 36) + (long long)P2 * (1 << 20) + (long long)P3 * 16 + (long long)(P4 >> 12);
 }
 // Integer finisher, ex = er + fc - 1014 (the biased exponent field of the result when W has its
