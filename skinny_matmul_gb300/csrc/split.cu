@@ -19,7 +19,8 @@
 //     magnitude <= 2^24: the FP32 accumulation in TMEM is exact.  Two accumulator sets alternate
 //     between periods, so the drain of one period runs while the MMAs of the next proceed.
 //   * Drain: TMEM -> int32; level sums S_L = sum_{i+j=L} D_ij (L = 2..9) are formed with a
-//     per-lane rotation and warp shuffles, then in shared memory with integer atomics;
+//     per-lane rotation and warp shuffles (all eight levels per shuffle stage), then in shared
+//     memory with integer atomics;
 //     V = sum_L S_L 2^(8(16-L)) is assembled from two int64 words and added to an FP64
 //     accumulator per C entry with weight 2^(EA+EB-2168).  Levels L >= 10 are dropped: their
 //     weight is below 2^-56 of the leading level (2^-52 with the headroom).
@@ -35,8 +36,9 @@
 //     The roles that wait most of the time (drain, producer, MMA) sleep between polls, so that
 //     their polling leaves issue slots to the slicers.  Every wait is bounded; a wait that runs
 //     out sets the error word, every role stops at its next wait, and the CTA writes no C.
-//   * Cross-CTA finish as in the CUDA-core kernel: CTA partials in FP64, the last CTA (ticket)
-//     sums them in CTA order, applies alpha/beta.
+//   * Cross-CTA finish in two levels: CTA partials in FP64; the last CTA of each group of 16
+//     (ticket) sums its group in CTA order, the last group sums the group sums in group order
+//     and applies alpha/beta (deterministic).
 // Inputs must be finite (Inf/NaN have no fixed-point form).
 
 #include <cstring>
