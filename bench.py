@@ -330,7 +330,7 @@ def kernel_of(it, method):
         wide = Mr > 16 or Nr > 16
         nblk = ((Mr + 63) // 64) * ((Nr + 63) // 64)
         auto_split = K >= 4096 and (Mr * Nr >= 256 or (Mr >= 8 and Nr >= 8)) and \
-            (not wide or Mr * Nr >= (160 if Mr <= 32 and Nr <= 32 else 320) * nblk)
+            (not wide or Mr * Nr >= (128 if Mr <= 32 and Nr <= 32 else 320) * nblk)
         if fp64 and (method == "split" or (method == "auto" and auto_split)):
             return "split_wide_kernel" if wide else "split_tsmttsm_kernel"
         p2 = lambda x: 1 << (x - 1).bit_length()

@@ -671,13 +671,14 @@ skinny_status split_tsmttsm_t(skinny_handle h, bool in_f32, bool out_f32, int64_
   // kernel is as fast or faster (4x16 0.71x, 4x32 0.44x).  The wide kernel costs about as much per 64 x 64
   // block whatever the block's fill (12.5 ms per block at K = 2^24; CUDA-core FP64 takes 23 ms at
   // M = N = 17 and 114 ms at 64), so it is chosen from M*N >= 320 per block on; with M, N <= 32 its
-  // folded stages halve that cost, and it wins from M*N >= 160 (1 GiB of operands: 20x8 1.9x,
-  // 17x17 2.1x, 32x8 1.8x; ties at 17x8 and 32x4).  The autotuner can override per shape.
+  // folded stages halve that cost, and with both widths >= 8 it wins from the smallest such
+  // product on (1 GiB of operands: 17x8 1.9x, 20x8 1.9x, 17x17 4.8x, 32x8 1.8x; 32x4 is a tie and
+  // takes the CUDA-core kernel through the rule above).  The autotuner can override per shape.
   const bool wide = M > 16 || N > 16;
   const int64_t sym_w = (A == B && lda == ldb && M == N) ? 1 : 0;
   const int64_t bm = (M + 63) / 64, bn = (N + 63) / 64;
   const int64_t nblk_w = sym_w ? bm * (bm + 1) / 2 : bm * bn;
-  const int64_t per_blk = (M <= 32 && N <= 32) ? 160 : 320;
+  const int64_t per_blk = (M <= 32 && N <= 32) ? 128 : 320;
   const bool narrow_wins = M * N >= 256 || (M >= 8 && N >= 8);
   if (autoselect && (K < 4096 || !narrow_wins || (wide && M * N < per_blk * nblk_w))) {
     set_error("split precision: not selected automatically for this shape");

@@ -88,6 +88,7 @@ struct Args {
   int beta_zero;
   int nblk, bm, sym;  // 64 x 64 blocks; sym: A == B, upper blocks only
   int bulk;           // rows by bulk copy (16-byte aligned rows of even width)
+  int abase16, bbase16;  // A / B start on a 16-byte boundary (dense stages by one bulk copy)
   int rstages;
   uint32_t raw_stage;  // bytes per FP64 stage
   int64_t nstages;     // ceil(K / rows per stage)
@@ -121,6 +122,11 @@ __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::befor
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// bytes a bulk copy will complete on the barrier, without an arrival
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
 }
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -233,7 +239,8 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
   const int nst = (int)(s_end - s_begin);
   const int R = p.rstages;
   // row strides (doubles) of the FP64 stages: dense operands land as one block of rows
-  const bool dense_a = p.bulk && p.lda == Mb, dense_b = p.bulk && ldb == Nb;
+  // dense operands (ld == block width, 16-byte aligned start): a stage's rows are one contiguous run
+  const bool dense_a = p.abase16 && p.lda == Mb, dense_b = (p.sym ? p.abase16 : p.bbase16) && ldb == Nb;
   // rows per stage; row stride of the stage's rows that are copied one by one (a folded stage
   // holds 32 rows of at most 32 values in the same 16 x 64 space)
   const int SR = FOLD ? 2 * ROWS : ROWS, rw = FOLD ? W / 2 : W;
@@ -292,21 +299,33 @@ __global__ void __launch_bounds__(THREADS, 1) split_wide_kernel(const Args p) {
           else
             bulk_g2s(dB + (r - na) * rw, Bb + (row0 + r - na) * ldb, (uint32_t)(Nb * ES), &raw_full[rs]);
         }
-      } else {  // rows not 16-byte aligned: element-sized asynchronous copies, one arrival per lane
-        for (int e = lane; e < rows * Mb; e += 32) {
-          const int r = e / Mb, c = e - r * Mb;
-          if constexpr (ES == 8)
-            cp_async8(dA + r * rw + c, Ab + (row0 + r) * p.lda + c);
-          else
-            cp_async4(dA + r * rw + c, Ab + (row0 + r) * p.lda + c);
+      } else {
+        // rows not all 16-byte aligned (odd widths or leading dimensions): a dense operand whose
+        // stage starts and ends on 16-byte boundaries (always but for an odd last stage) is one
+        // bulk copy, announced on the barrier without an arrival; the rest element by element;
+        // one arrival per lane once its element copies have landed
+        const bool sa = dense_a && (row0 * Mb * ES) % 16 == 0 && (rows * Mb * ES) % 16 == 0;
+        const bool sb = !gram && dense_b && (row0 * Nb * ES) % 16 == 0 && (rows * Nb * ES) % 16 == 0;
+        if (lane == 0 && (sa || sb)) {
+          mbar_expect_tx(&raw_full[rs], (uint32_t)(((sa ? rows * Mb : 0) + (sb ? rows * Nb : 0)) * ES));
+          if (sa) bulk_g2s(dA, Ab + row0 * p.lda, (uint32_t)(rows * Mb * ES), &raw_full[rs]);
+          if (sb) bulk_g2s(dB, Bb + row0 * ldb, (uint32_t)(rows * Nb * ES), &raw_full[rs]);
         }
-        if (!gram)
+        if (!sa)
+          for (int e = lane; e < rows * Mb; e += 32) {
+            const int r = e / Mb, c = e - r * Mb;
+            if constexpr (ES == 8)
+              cp_async8(dA + r * rsa + c, Ab + (row0 + r) * p.lda + c);
+            else
+              cp_async4(dA + r * rsa + c, Ab + (row0 + r) * p.lda + c);
+          }
+        if (!gram && !sb)
           for (int e = lane; e < rows * Nb; e += 32) {
             const int r = e / Nb, c = e - r * Nb;
             if constexpr (ES == 8)
-              cp_async8(dB + r * rw + c, Bb + (row0 + r) * ldb + c);
+              cp_async8(dB + r * rsb + c, Bb + (row0 + r) * ldb + c);
             else
-              cp_async4(dB + r * rw + c, Bb + (row0 + r) * ldb + c);
+              cp_async4(dB + r * rsb + c, Bb + (row0 + r) * ldb + c);
           }
         cp_async_arrive(&raw_full[rs]);
       }
@@ -697,6 +716,8 @@ skinny_status split_wide_t(skinny_handle h, bool in_f32, bool out_f32, int64_t M
   const bool aligned =
       (uintptr_t)A % 16 == 0 && (uintptr_t)B % 16 == 0 && lda % per16 == 0 && ldb % per16 == 0;
   a.bulk = aligned && M % per16 == 0 && N % per16 == 0;
+  a.abase16 = (uintptr_t)A % 16 == 0;
+  a.bbase16 = (uintptr_t)B % 16 == 0;
   a.raw_stage = (a.sym && a.nblk == 1) ? RAW_OP : 2 * RAW_OP;
   const bool fold = M <= W / 2 && N <= W / 2;  // 32-row stages folded into the 64-row planes
   const int64_t fixed = HDR + (int64_t)DSLOTS * SLOT;
